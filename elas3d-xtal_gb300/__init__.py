@@ -1,0 +1,427 @@
+"""GB300 (sm_103a) voxel-FE elasticity solver -- host API.
+
+A drop-in for the hot path of ELAS3D-Xtal (src/elas3dxtal_pcg.f90): the
+matrix-free voxel finite-element PCG solve.  The compute runs in the CUDA
+library ``_build/libe3d_gpu.so`` behind the C ABI of ``include/e3d_gpu.h``;
+this module binds it with ctypes and mirrors the reference's subroutines on
+its shared data type ``e3d``:
+
+    reference (src/elas3dxtal_pcg.f90)      here (class Elas3D)
+    ppixel_hdf5            :2879            upload(pix, rodrigues)
+    femat_OpenMP           :555             femat()
+    affine guess (driver)  :423             init_affine()
+    energy_OpenMP          :1107            energy() -> (utot, gg)
+    dembx_OpenMP           :1356            dembx() -> stats
+    stress_OpenMP          :2149            stress() -> (strav, epsav)
+    stress_fullfield_OpenMP:2639            stress_fullfield() -> (sigma, vm)
+    assig                  :2410            assig(pix, nphase)
+    program elas3d         :186             run()
+
+There is no CPU fallback: if the library or a CUDA device is missing the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libe3d_gpu.so")
+
+E3D_OK = 0
+E3D_ERR_INPUT = 1
+E3D_ERR_OOM = 2
+E3D_ERR_BREAKDOWN = 3
+E3D_ERR_MAXITER = 4
+E3D_ERR_TIMEOUT = 5
+E3D_ERR_CUDA = 6
+E3D_ERR_STATE = 7
+
+EXIT_CONVERGED, EXIT_HAH_GUARD, EXIT_MAXITER, EXIT_BREAKDOWN, EXIT_TIMEOUT, EXIT_RUNNING = range(6)
+CRIT_REF, CRIT_PRECOND_REL = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+# Every symbol include/e3d_gpu.h and include/e3d_micro.h declare.
+EXPORTED_SYMBOLS = (
+    "e3d_problem_defaults", "e3d_create", "e3d_destroy", "e3d_upload", "e3d_femat",
+    "e3d_init_affine", "e3d_energy", "e3d_solve", "e3d_solve_begin", "e3d_iterate",
+    "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
+    "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
+    "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
+    "e3d_device_bytes", "e3d_launch_count", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
+    "e3d_euler_to_rodrigues",
+)
+
+
+class E3DError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        msg = f"{what}: {strerror(code)} (E3D status {code})"
+        if code == E3D_ERR_CUDA:
+            msg += f" [{last_cuda_error()}]"
+        super().__init__(msg)
+
+
+class ProblemC(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("nphase", C.c_int32),
+        ("flag_m", C.c_int32), ("criterion", C.c_int32), ("precision", C.c_int32),
+        ("divergence_reset", C.c_int32), ("max_iter", C.c_int32), ("device", C.c_int32),
+        ("tol", C.c_float), ("refine_every", C.c_int32),
+        ("c11", C.c_double), ("c12", C.c_double), ("c44", C.c_double),
+        ("e1", C.c_double), ("nu1", C.c_double), ("strain", C.c_double * 6),
+        ("hbm_budget", C.c_int64),
+    ]
+
+
+class SolveStatsC(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32), ("exit_reason", C.c_int32), ("resets", C.c_int32),
+        ("refinements", C.c_int32), ("gg", C.c_double), ("gg0", C.c_double),
+        ("rel_res", C.c_double), ("true_rel", C.c_double), ("ms_setup", C.c_double),
+        ("ms_iter", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with elas3d-xtal_gb300/build.py "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(p)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    L.e3d_problem_defaults.argtypes = [C.POINTER(ProblemC), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.e3d_problem_defaults.restype = None
+    L.e3d_create.argtypes = [C.POINTER(vp), C.POINTER(ProblemC)]
+    for name in ("e3d_destroy", "e3d_femat", "e3d_init_affine", "e3d_solve_begin"):
+        getattr(L, name).argtypes = [vp]
+    L.e3d_upload.argtypes = [vp, ip, dp]
+    L.e3d_energy.argtypes = [vp, dp, dp]
+    L.e3d_solve.argtypes = [vp, C.POINTER(SolveStatsC)]
+    L.e3d_iterate.argtypes = [vp, C.c_int32, C.POINTER(SolveStatsC)]
+    L.e3d_stress.argtypes = [vp, dp, dp]
+    L.e3d_stress_field.argtypes = [vp, dp, dp]
+    L.e3d_run.argtypes = [vp, dp, dp, C.POINTER(SolveStatsC)]
+    L.e3d_apply.argtypes = [vp, dp, dp]
+    L.e3d_apply_device.argtypes = [vp, vp, vp]
+    for name in ("e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C",
+                 "e3d_get_cmod", "e3d_get_dk", "e3d_get_minv"):
+        getattr(L, name).argtypes = [vp, dp]
+    L.e3d_get_history.argtypes = [vp, dp, C.c_int32, ip]
+    L.e3d_device_ptrs.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+    L.e3d_device_bytes.argtypes = [vp]
+    L.e3d_device_bytes.restype = C.c_int64
+    L.e3d_launch_count.argtypes = [vp]
+    L.e3d_launch_count.restype = C.c_int64
+    L.e3d_strerror.argtypes = [C.c_int32]
+    L.e3d_strerror.restype = C.c_char_p
+    L.e3d_last_cuda_error.argtypes = []
+    L.e3d_last_cuda_error.restype = C.c_char_p
+    L.e3d_micro_grains.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
+                                   ip, dp]
+    L.e3d_micro_spherical_pores.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                            C.c_double, C.c_int32, C.c_uint64, ip]
+    L.e3d_micro_ellipsoidal_pores.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_int32, C.c_uint64, ip]
+    L.e3d_euler_to_rodrigues.argtypes = [C.c_int32, dp, dp]
+    L.e3d_euler_to_rodrigues.restype = None
+    for name in EXPORTED_SYMBOLS:
+        fn = getattr(L, name)
+        if fn.restype is C.c_int and name not in ("e3d_problem_defaults", "e3d_euler_to_rodrigues"):
+            fn.restype = C.c_int32
+    if path is None:
+        _lib = L
+    return L
+
+
+def strerror(code: int) -> str:
+    try:
+        return load_library().e3d_strerror(code).decode()
+    except Exception:  # library missing: still produce a message
+        return f"status {code}"
+
+
+def last_cuda_error() -> str:
+    try:
+        return load_library().e3d_last_cuda_error().decode()
+    except Exception:
+        return ""
+
+
+def _check(rc: int, what: str, allow=()):
+    if rc != E3D_OK and rc not in allow:
+        raise E3DError(rc, what)
+    return rc
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+@dataclass
+class Problem:
+    """Runtime form of the reference's compile-time constants
+    (src/elas3dxtal_pcg.f90:77-148).  Strains are tensor components."""
+    nx: int
+    ny: int
+    nz: int
+    nphase: int
+    flag_m: int = 1
+    c11: float = 206.0e9
+    c12: float = 133.0e9
+    c44: float = 119.0e9
+    e1: float = 0.0
+    nu1: float = 0.0
+    strain: tuple = (0.0, 0.0, 1.0e-3, 0.0, 0.0, 0.0)  # exx eyy ezz exz eyz exy
+    tol: float = 1.0e-8
+    max_iter: int = 10000
+    criterion: int = CRIT_REF
+    precision: int = PREC_FP64
+    divergence_reset: int = 1
+    refine_every: int = 0
+    device: int = 0
+    hbm_budget: int = 0
+
+    @property
+    def ns(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def to_c(self) -> ProblemC:
+        p = ProblemC()
+        p.nx, p.ny, p.nz, p.nphase = self.nx, self.ny, self.nz, self.nphase
+        p.flag_m, p.criterion, p.precision = self.flag_m, self.criterion, self.precision
+        p.divergence_reset, p.max_iter, p.device = self.divergence_reset, self.max_iter, self.device
+        p.tol, p.refine_every = self.tol, self.refine_every
+        p.c11, p.c12, p.c44, p.e1, p.nu1 = self.c11, self.c12, self.c44, self.e1, self.nu1
+        for i in range(6):
+            p.strain[i] = float(self.strain[i])
+        p.hbm_budget = int(self.hbm_budget)
+        return p
+
+
+class Elas3D:
+    """One problem on one GPU (the reference's ``type(elas3d_data_type) :: e3d``)."""
+
+    def __init__(self, problem: Problem):
+        self.p = problem
+        self.L = load_library()
+        self._h = C.c_void_p()
+        pc = problem.to_c()
+        _check(self.L.e3d_create(C.byref(self._h), C.byref(pc)), "e3d_create")
+
+    # -- lifecycle
+    def close(self):
+        if self._h:
+            self.L.e3d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- inputs (ppixel_hdf5)
+    def upload(self, pix: np.ndarray, rodrigues: np.ndarray | None):
+        pix = np.ascontiguousarray(pix, dtype=np.int32).reshape(-1)
+        if pix.size != self.p.ns:
+            raise ValueError(f"pix has {pix.size} entries, expected ns = {self.p.ns}")
+        rod = None
+        if rodrigues is not None and self.p.nphase > 1:
+            rod = np.ascontiguousarray(rodrigues, dtype=np.float64).reshape(-1)
+            if self.p.flag_m == 1 and rod.size != 3 * (self.p.nphase - 1):
+                raise ValueError(f"orientation has {rod.size} entries, expected {3 * (self.p.nphase - 1)}")
+        _check(self.L.e3d_upload(self._h, _ip(pix), _dp(rod) if rod is not None else None), "e3d_upload")
+        return self
+
+    # -- reference subroutines
+    def femat(self):
+        _check(self.L.e3d_femat(self._h), "e3d_femat")
+        return self
+
+    def init_affine(self):
+        _check(self.L.e3d_init_affine(self._h), "e3d_init_affine")
+        return self
+
+    def energy(self):
+        ut = C.c_double()
+        gg = C.c_double()
+        _check(self.L.e3d_energy(self._h, C.byref(ut), C.byref(gg)), "e3d_energy")
+        return ut.value, gg.value
+
+    def dembx(self) -> dict:
+        st = SolveStatsC()
+        rc = self.L.e3d_solve(self._h, C.byref(st))
+        _check(rc, "e3d_solve", allow=(E3D_ERR_MAXITER,))
+        d = st.as_dict()
+        d["status"] = rc
+        return d
+
+    solve = dembx
+
+    def solve_begin(self):
+        _check(self.L.e3d_solve_begin(self._h), "e3d_solve_begin")
+
+    def iterate(self, n: int) -> dict:
+        st = SolveStatsC()
+        _check(self.L.e3d_iterate(self._h, int(n), C.byref(st)), "e3d_iterate")
+        return st.as_dict()
+
+    def stress(self):
+        s = np.zeros(6)
+        e = np.zeros(6)
+        _check(self.L.e3d_stress(self._h, _dp(s), _dp(e)), "e3d_stress")
+        return s, e
+
+    def stress_fullfield(self):
+        sig = np.zeros(6 * self.p.ns)
+        vm = np.zeros(self.p.ns)
+        _check(self.L.e3d_stress_field(self._h, _dp(sig), _dp(vm)), "e3d_stress_field")
+        return sig, vm
+
+    def run(self) -> dict:
+        ut = np.zeros(2)
+        out = np.zeros(12)
+        st = SolveStatsC()
+        rc = self.L.e3d_run(self._h, _dp(ut), _dp(out), C.byref(st))
+        _check(rc, "e3d_run", allow=(E3D_ERR_MAXITER,))
+        d = st.as_dict()
+        d.update(status=rc, utot0=ut[0], utot=ut[1], strav=out[:6].copy(), epsav=out[6:].copy())
+        return d
+
+    # -- test hooks and state transfer
+    def apply(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        if x.size != 3 * self.p.ns:
+            raise ValueError("x must have 3*ns entries")
+        y = np.empty_like(x)
+        _check(self.L.e3d_apply(self._h, _dp(x), _dp(y)), "e3d_apply")
+        return y
+
+    def _get(self, fn, n):
+        out = np.empty(n)
+        _check(fn(self._h, _dp(out)), fn.__name__)
+        return out
+
+    def set_u(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        _check(self.L.e3d_set_u(self._h, _dp(u)), "e3d_set_u")
+
+    def get_u(self):
+        return self._get(self.L.e3d_get_u, 3 * self.p.ns)
+
+    def get_g(self):
+        return self._get(self.L.e3d_get_g, 3 * self.p.ns)
+
+    def get_b(self):
+        return self._get(self.L.e3d_get_b, 3 * self.p.ns)
+
+    def get_C(self) -> float:
+        v = C.c_double()
+        _check(self.L.e3d_get_C(self._h, C.byref(v)), "e3d_get_C")
+        return v.value
+
+    def get_cmod(self):
+        """cmod as [p, i, j]."""
+        raw = self._get(self.L.e3d_get_cmod, 36 * self.p.nphase)
+        return raw.reshape(6, 6, self.p.nphase).transpose(2, 1, 0)
+
+    def get_dk(self):
+        """dk as [p, a, i, b, j] (reference local node order, 0-based)."""
+        raw = self._get(self.L.e3d_get_dk, 576 * self.p.nphase)
+        return raw.reshape(3, 8, 3, 8, self.p.nphase).transpose(4, 3, 2, 1, 0)
+
+    def get_minv(self):
+        """M_block_inv(ns,3,3) as [m, i, j]."""
+        raw = self._get(self.L.e3d_get_minv, 9 * self.p.ns)
+        return raw.reshape(3, 3, self.p.ns).transpose(2, 1, 0)
+
+    def history(self) -> np.ndarray:
+        n = max(self.p.max_iter, 1)
+        out = np.zeros(n)
+        cnt = C.c_int32()
+        _check(self.L.e3d_get_history(self._h, _dp(out), n, C.byref(cnt)), "e3d_get_history")
+        return out[: cnt.value].copy()
+
+    def device_bytes(self) -> int:
+        return int(self.L.e3d_device_bytes(self._h))
+
+    def launch_count(self) -> int:
+        return int(self.L.e3d_launch_count(self._h))
+
+
+def assig(pix: np.ndarray, nphase: int) -> np.ndarray:
+    """Phase volume fractions (assig, src/elas3dxtal_pcg.f90:2410-2468)."""
+    pix = np.asarray(pix).reshape(-1)
+    ok = (pix >= 1) & (pix <= nphase)
+    return np.bincount(pix[ok] - 1, minlength=nphase)[:nphase] / float(pix.size)
+
+
+# ---------------------------------------------------------------------------
+# Synthetic microstructures (include/e3d_micro.h)
+def micro_grains(nx, ny, nz, ngrains, seed, laguerre_sigma=0.0):
+    L = load_library()
+    pix = np.empty(nx * ny * nz, np.int32)
+    rod = np.empty(3 * ngrains)
+    rc = L.e3d_micro_grains(nx, ny, nz, ngrains, float(laguerre_sigma), int(seed) & (2**64 - 1),
+                            _ip(pix), _dp(rod))
+    if rc != 0:
+        raise RuntimeError(f"e3d_micro_grains failed ({rc})")
+    return pix, rod
+
+
+def micro_spherical_pores(pix, nx, ny, nz, frac, pore_phase, seed, log_mu=np.log(3.0), log_sigma=0.4):
+    L = load_library()
+    assert pix.dtype == np.int32 and pix.flags.c_contiguous
+    rc = L.e3d_micro_spherical_pores(nx, ny, nz, float(frac), float(log_mu), float(log_sigma),
+                                     int(pore_phase), int(seed) & (2**64 - 1), _ip(pix))
+    if rc < 0:
+        raise RuntimeError(f"e3d_micro_spherical_pores failed ({rc})")
+    return rc
+
+
+def micro_ellipsoidal_pores(pix, nx, ny, nz, frac, pore_phase, seed, aspect=4.0,
+                            log_mu=np.log(2.0), log_sigma=0.3):
+    L = load_library()
+    assert pix.dtype == np.int32 and pix.flags.c_contiguous
+    rc = L.e3d_micro_ellipsoidal_pores(nx, ny, nz, float(frac), float(aspect), float(log_mu),
+                                       float(log_sigma), int(pore_phase), int(seed) & (2**64 - 1),
+                                       _ip(pix))
+    if rc < 0:
+        raise RuntimeError(f"e3d_micro_ellipsoidal_pores failed ({rc})")
+    return rc
+
+
+def euler_to_rodrigues(euler: np.ndarray) -> np.ndarray:
+    e = np.ascontiguousarray(euler, dtype=np.float64).reshape(-1)
+    out = np.empty_like(e)
+    load_library().e3d_euler_to_rodrigues(e.size // 3, _dp(e), _dp(out))
+    return out

@@ -1,0 +1,78 @@
+"""Build recipe for the sm_103a library (in-tree, no cmake).
+
+Produces ``elas3d-xtal_gb300/_build/libe3d_gpu.so`` from
+``csrc/e3d_gpu.cu`` (nvcc, ``-gencode arch=compute_103a,code=sm_103a``) and
+``csrc/microgen.cpp`` (g++, portable flags so the same recipe builds on x86-64
+and AArch64).  Translation units compile in parallel; the step is skipped when
+the library is newer than every source.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT, "libe3d_gpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build the library")
+    return cand
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
+            if f.endswith((".cu", ".cuh", ".cpp", ".h"))] + \
+           [os.path.join(INCLUDE, f) for f in sorted(os.listdir(INCLUDE)) if f.endswith(".h")]
+
+
+def up_to_date() -> bool:
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    cu_obj = os.path.join(OUT, "e3d_gpu.o")
+    cpp_obj = os.path.join(OUT, "microgen.o")
+    cu_cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, "e3d_gpu.cu"), "-o", cu_obj]
+    if ptxas_info:
+        cu_cmd[1:1] = ["-Xptxas", "-v"]
+    cpp_cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I", INCLUDE,
+               "-c", os.path.join(CSRC, "microgen.cpp"), "-o", cpp_obj]
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        return r.stdout + r.stderr
+
+    with ThreadPoolExecutor(2) as ex:
+        logs = list(ex.map(run, [cu_cmd, cpp_cmd]))
+    link = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", cu_obj, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
+    logs.append(run(link))
+    os.replace(LIB + ".tmp", LIB)
+    if verbose or ptxas_info:
+        sys.stdout.write("".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True, ptxas_info="-v" in sys.argv)
+    print(LIB)

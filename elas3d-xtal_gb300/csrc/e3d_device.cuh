@@ -1,0 +1,208 @@
+// Device-side building blocks of the sm_103a voxel-FE solver.
+//
+// Element arithmetic.  The reference integrates the 24x24 element matrix
+// dk = sum_q w_q B_q^T C B_q over 3x3x3 Simpson points
+// (src/elas3dxtal_pcg.f90:713-805) and applies it node by node with 576
+// multiply-adds (:1176-1321).  The integrand is at most quadratic in each
+// coordinate, so that rule is exact, and so is the 2x2x2 Gauss rule.  Under the
+// Gauss rule the strain field of a trilinear element splits into 7 mutually
+// orthogonal modes (constant, x, y, z, xy, xz, yz), so
+//     K_e u = H^T [ sum_k W_k M_k^T C M_k ] H u,
+// with H the 8-point Walsh-Hadamard transform of the nodal values, M_k a
+// sparse selector and W = 1/16, 1/48, 1/144.  That is the same matrix to
+// rounding (checked against the Simpson dk to 4e-16) at ~276 FP64 operations
+// per element instead of 576.  GB300 runs FP64 at 1/64 of its FP32 rate, so
+// the stencil is FP64-issue-bound and this count, not HBM bytes, sets its time.
+//
+// Corner index inside an element: a = ox + 2*oy + 4*oz.  Hadamard index
+// b = bx + 2*by + 4*bz (bit set = difference along that axis).
+#pragma once
+#include <cstdint>
+
+namespace e3d {
+
+enum : int { HX_ = 1, HY_ = 2, HXY = 3, HZ_ = 4, HXZ = 5, HYZ = 6, HXYZ = 7 };
+
+// Scaled stiffness table per phase: C/16, C/48, C/144 (row-major 6x6 each).
+constexpr int kCsStride = 108;
+
+template <typename T>
+__device__ __forceinline__ T fma_(T a, T b, T c) {
+  return fma(a, b, c);
+}
+
+// s[r] = sum_c C[r][c] e[c] for r, c in the index set IDX (N entries).
+template <typename T, int N>
+__device__ __forceinline__ void matvec_sub(const T* __restrict__ Cm, const int (&idx)[N],
+                                           const T (&e)[N], T (&s)[N]) {
+#pragma unroll
+  for (int r = 0; r < N; ++r) {
+    T acc = Cm[6 * idx[r] + idx[0]] * e[0];
+#pragma unroll
+    for (int c = 1; c < N; ++c) acc = fma_(Cm[6 * idx[r] + idx[c]], e[c], acc);
+    s[r] = acc;
+  }
+}
+
+// Element forces in the Hadamard domain: (hu, hv, hw) -> (fu, fv, fw).
+// cs points at the phase's 108-entry scaled stiffness.
+template <typename T>
+__device__ __forceinline__ void element_modal(const T* __restrict__ cs, const T (&hu)[8],
+                                              const T (&hv)[8], const T (&hw)[8], T (&fu)[8],
+                                              T (&fv)[8], T (&fw)[8]) {
+  const T* C0 = cs;
+  const T* C1 = cs + 36;
+  const T* C2 = cs + 72;
+  // constant mode, all six Voigt components (xx, yy, zz, xz, yz, xy)
+  {
+    const int idx[6] = {0, 1, 2, 3, 4, 5};
+    const T e[6] = {hu[HX_], hv[HY_], hw[HZ_], hu[HZ_] + hw[HX_], hv[HZ_] + hw[HY_], hu[HY_] + hv[HX_]};
+    T s[6];
+    matvec_sub<T, 6>(C0, idx, e, s);
+    fu[HX_] = s[0];
+    fv[HY_] = s[1];
+    fw[HZ_] = s[2];
+    fu[HZ_] = s[3];
+    fw[HX_] = s[3];
+    fv[HZ_] = s[4];
+    fw[HY_] = s[4];
+    fu[HY_] = s[5];
+    fv[HX_] = s[5];
+  }
+  T sx[5], sy[5], sz[5];
+  {  // x mode: yy, zz, xz, yz, xy
+    const int idx[5] = {1, 2, 3, 4, 5};
+    const T e[5] = {hv[HXY], hw[HXZ], hu[HXZ], hv[HXZ] + hw[HXY], hu[HXY]};
+    matvec_sub<T, 5>(C1, idx, e, sx);
+  }
+  {  // y mode: xx, zz, xz, yz, xy
+    const int idx[5] = {0, 2, 3, 4, 5};
+    const T e[5] = {hu[HXY], hw[HYZ], hu[HYZ] + hw[HXY], hv[HYZ], hv[HXY]};
+    matvec_sub<T, 5>(C1, idx, e, sy);
+  }
+  {  // z mode: xx, yy, xz, yz, xy
+    const int idx[5] = {0, 1, 3, 4, 5};
+    const T e[5] = {hu[HXZ], hv[HYZ], hw[HXZ], hw[HYZ], hu[HYZ] + hv[HXZ]};
+    matvec_sub<T, 5>(C1, idx, e, sz);
+  }
+  // sx = [yy, zz, xz, yz, xy]; sy = [xx, zz, xz, yz, xy]; sz = [xx, yy, xz, yz, xy]
+  fu[HXY] = sx[4] + sy[0];
+  fv[HXY] = sx[0] + sy[4];
+  fw[HXY] = sx[3] + sy[2];
+  fu[HXZ] = sx[2] + sz[0];
+  fv[HXZ] = sx[3] + sz[4];
+  fw[HXZ] = sx[1] + sz[2];
+  fu[HYZ] = sy[2] + sz[4];
+  fv[HYZ] = sy[3] + sz[1];
+  fw[HYZ] = sy[1] + sz[3];
+  T sxy[3], sxz[3], syz[3];
+  {  // xy mode: zz, xz, yz
+    const int idx[3] = {2, 3, 4};
+    const T e[3] = {hw[HXYZ], hu[HXYZ], hv[HXYZ]};
+    matvec_sub<T, 3>(C2, idx, e, sxy);
+  }
+  {  // xz mode: yy, yz, xy
+    const int idx[3] = {1, 4, 5};
+    const T e[3] = {hv[HXYZ], hw[HXYZ], hu[HXYZ]};
+    matvec_sub<T, 3>(C2, idx, e, sxz);
+  }
+  {  // yz mode: xx, xz, xy
+    const int idx[3] = {0, 3, 5};
+    const T e[3] = {hu[HXYZ], hw[HXYZ], hv[HXYZ]};
+    matvec_sub<T, 3>(C2, idx, e, syz);
+  }
+  fu[HXYZ] = sxy[1] + sxz[2] + syz[0];
+  fv[HXYZ] = sxy[2] + sxz[0] + syz[2];
+  fw[HXYZ] = sxy[0] + sxz[1] + syz[1];
+  fu[0] = T(0);
+  fv[0] = T(0);
+  fw[0] = T(0);
+}
+
+// Forward Hadamard of one plane of 4 corner values v[oy*2+ox] -> P[by*2+bx].
+template <typename T>
+__device__ __forceinline__ void had_xy(const T (&v)[4], T (&P)[4]) {
+  const T s0 = v[1] + v[0], d0 = v[1] - v[0];
+  const T s1 = v[3] + v[2], d1 = v[3] - v[2];
+  P[0] = s1 + s0;
+  P[2] = s1 - s0;
+  P[1] = d1 + d0;
+  P[3] = d1 - d0;
+}
+
+// Adjoint of had_xy: T[by*2+bx] -> corner forces r[oy*2+ox].
+template <typename T>
+__device__ __forceinline__ void had_xy_adj(const T (&Tm)[4], T (&r)[4]) {
+  const T e0 = Tm[0] - Tm[2], e1 = Tm[0] + Tm[2];
+  const T g0 = Tm[1] - Tm[3], g1 = Tm[1] + Tm[3];
+  r[0] = e0 - g0;
+  r[1] = e0 + g0;
+  r[2] = e1 - g1;
+  r[3] = e1 + g1;
+}
+
+// Full element: 8 corner values per component (a = ox + 2oy + 4oz) -> forces.
+// Used by the one-off kernels (dk build, boundary terms, tests of the tile path).
+template <typename T>
+__device__ __forceinline__ void element_apply(const T* __restrict__ cs, const T (&u)[3][8],
+                                              T (&r)[3][8]) {
+  T h[3][8];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const T lo[4] = {u[c][0], u[c][1], u[c][2], u[c][3]};
+    const T hi[4] = {u[c][4], u[c][5], u[c][6], u[c][7]};
+    T Plo[4], Phi[4];
+    had_xy(lo, Plo);
+    had_xy(hi, Phi);
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      h[c][b] = Phi[b] + Plo[b];
+      h[c][b + 4] = Phi[b] - Plo[b];
+    }
+  }
+  T f[3][8];
+  element_modal<T>(cs, h[0], h[1], h[2], f[0], f[1], f[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    T tlo[4], thi[4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      tlo[b] = f[c][b] - f[c][b + 4];
+      thi[b] = f[c][b] + f[c][b + 4];
+    }
+    T rlo[4], rhi[4];
+    had_xy_adj(tlo, rlo);
+    had_xy_adj(thi, rhi);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      r[c][a] = rlo[a];
+      r[c][a + 4] = rhi[a];
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Block-wide sum of one value per thread (fixed shuffle + shared-memory tree,
+// so the result does not depend on scheduling).  Result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NT / 32; ++i) s += scratch[i];
+  }
+  return s;
+}
+
+}  // namespace e3d

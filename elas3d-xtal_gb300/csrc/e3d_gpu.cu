@@ -1,0 +1,727 @@
+// C ABI of the sm_103a voxel-FE solver (include/e3d_gpu.h).  Each entry point
+// replaces one subroutine of src/elas3dxtal_pcg.f90; see the header for the
+// mapping.  All device work runs on the handle's stream; calls return after it
+// completes.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "e3d_gpu.h"
+#include "e3d_kernels.cuh"
+
+using namespace e3d;
+
+namespace {
+
+thread_local std::string g_last_cuda_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct e3d_handle {
+  e3d_problem_t prob{};
+  GridDims G{};
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int64_t bytes = 0;
+  int64_t launches = 0;
+  std::vector<void*> allocs;
+
+  // state (see e3d_kernels.cuh for the layout)
+  int32_t* pix = nullptr;
+  double* rod = nullptr;
+  double* cmod = nullptr;
+  double* cs = nullptr;
+  float* cs32 = nullptr;
+  double* dk = nullptr;
+  double* dkd = nullptr;
+  double* u = nullptr;
+  double* g = nullptr;
+  double* b = nullptr;
+  double* z = nullptr;
+  double* h0 = nullptr;
+  double* h1 = nullptr;
+  double* Ah = nullptr;
+  double* minv = nullptr;
+  double* hx = nullptr;
+  double* hy = nullptr;
+  double* hd = nullptr;
+  double* partial = nullptr;  // reduction scratch
+  int partial_n = 0;
+  double* scalars = nullptr;  // small results
+  double* history = nullptr;
+  PcgState* st = nullptr;
+  GridBarrier* bar = nullptr;
+  int* err = nullptr;
+
+  double C = 0.0;
+  double gg0 = 0.0;
+  bool uploaded = false, femat_done = false, energy_done = false, solve_ready = false, minv_ready = false;
+  int pcg_grid = 0;
+  double ms_setup = 0.0, ms_iter = 0.0;
+  JumpParams J{};
+};
+
+namespace {
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  g_last_cuda_error = buf;
+  return E3D_ERR_CUDA;
+}
+
+#define E3D_CUDA(call)                                 \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+#define E3D_LAUNCHED(h)                                          \
+  do {                                                           \
+    (h)->launches++;                                             \
+    cudaError_t e_ = cudaGetLastError();                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, "kernel launch"); \
+  } while (0)
+
+template <typename T>
+int32_t dalloc(e3d_handle* h, T** p, size_t count) {
+  const size_t bytes = count * sizeof(T) + 16;
+  if (h->prob.hbm_budget > 0 && h->bytes + (int64_t)bytes > h->prob.hbm_budget) return E3D_ERR_OOM;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return E3D_ERR_OOM;
+  }
+  h->allocs.push_back(q);
+  h->bytes += (int64_t)bytes;
+  *p = static_cast<T*>(q);
+  return E3D_OK;
+}
+
+int32_t sync(e3d_handle* h) {
+  E3D_CUDA(cudaStreamSynchronize(h->stream));
+  int derr = 0;
+  E3D_CUDA(cudaMemcpy(&derr, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (derr == DEV_TIMEOUT) return E3D_ERR_TIMEOUT;
+  if (derr != DEV_OK) return E3D_ERR_CUDA;
+  return E3D_OK;
+}
+
+unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+int reduction_grid(const e3d_handle* h) { return std::max(1, std::min(h->num_sms * 4, h->partial_n)); }
+
+// Sum `nfields` interleaved fields of n partials into h->scalars[0..nfields).
+int32_t reduce_to_host(e3d_handle* h, int n, int stride, int nfields, double* out) {
+  reduce_partials_kernel<<<1, 256, 0, h->stream>>>(h->partial, n, stride, nfields, h->scalars);
+  E3D_LAUNCHED(h);
+  E3D_CUDA(cudaMemcpyAsync(out, h->scalars, sizeof(double) * nfields, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+ApplyArgs<double> apply_args(e3d_handle* h, const double* x, double* y) {
+  ApplyArgs<double> A{};
+  A.g = h->G;
+  A.pix = h->pix;
+  A.cs = h->cs;
+  A.x = x;
+  A.zv = nullptr;
+  A.gamma = 0.0;
+  A.reset = 0;
+  A.hnew = nullptr;
+  A.y = y;
+  A.hx = h->hx;
+  A.hy = h->hy;
+  A.hd = h->hd;
+  return A;
+}
+
+// y_partial = in-tile K x plus halos (not yet added).
+int32_t launch_apply_tiles(e3d_handle* h, const double* x, double* y) {
+  ApplyArgs<double> A = apply_args(h, x, y);
+  apply_tiles_kernel<double><<<(unsigned)h->G.ntiles, NT, 0, h->stream>>>(A, nullptr);
+  E3D_LAUNCHED(h);
+  return E3D_OK;
+}
+
+int32_t apply_device(e3d_handle* h, const double* d_x, double* d_y) {
+  int32_t rc = launch_apply_tiles(h, d_x, h->Ah);
+  if (rc) return rc;
+  apply_finish_kernel<double><<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->Ah, h->hx, h->hy,
+                                                                                 h->hd, d_y);
+  E3D_LAUNCHED(h);
+  return E3D_OK;
+}
+
+GridDims make_dims(int nx, int ny, int nz, int num_sms) {
+  GridDims G{};
+  G.nx = nx;
+  G.ny = ny;
+  G.nz = nz;
+  G.ns = (long long)nx * ny * nz;
+  G.ntx = (nx + TILE_X - 1) / TILE_X;
+  G.nty = (ny + TILE_Y - 1) / TILE_Y;
+  // z chunk: keep >= ~16 tiles per SM in flight (load balance) but long
+  // enough that the one redundant element plane per chunk stays small.
+  const long long cols = (long long)G.ntx * G.nty;
+  const long long want = std::max<long long>(1, (long long)num_sms * 16);
+  int ntz = (int)std::max<long long>(1, std::min<long long>(nz, (want + cols - 1) / cols));
+  int tz = (nz + ntz - 1) / ntz;
+  if (tz < 16) tz = std::min(nz, 16);
+  G.tz = tz;
+  G.ntz = (nz + tz - 1) / tz;
+  G.ntiles = cols * G.ntz;
+  return G;
+}
+
+}  // namespace
+
+extern "C" {
+
+void e3d_problem_defaults(e3d_problem_t* p, int32_t nx, int32_t ny, int32_t nz, int32_t nphase) {
+  std::memset(p, 0, sizeof *p);
+  p->nx = nx;
+  p->ny = ny;
+  p->nz = nz;
+  p->nphase = nphase;
+  p->flag_m = 1;
+  p->criterion = E3D_CRIT_REF;
+  p->precision = E3D_PREC_FP64;
+  p->divergence_reset = 1;
+  p->max_iter = 10000;
+  p->device = 0;
+  p->tol = 1.0e-8f;
+  p->refine_every = 0;
+  p->c11 = 206.0e9;
+  p->c12 = 133.0e9;
+  p->c44 = 119.0e9;
+  p->e1 = 0.0;
+  p->nu1 = 0.0;
+  p->strain[2] = 1.0e-3;
+  p->hbm_budget = 0;
+}
+
+const char* e3d_strerror(int32_t s) {
+  switch (s) {
+    case E3D_OK: return "ok";
+    case E3D_ERR_INPUT: return "invalid input";
+    case E3D_ERR_OOM: return "device memory exhausted or over the HBM budget";
+    case E3D_ERR_BREAKDOWN: return "PCG breakdown (non-finite h.Ah or z.g)";
+    case E3D_ERR_MAXITER: return "maximum iterations reached without convergence";
+    case E3D_ERR_TIMEOUT: return "device-side wait exceeded its limit";
+    case E3D_ERR_CUDA: return "CUDA runtime error";
+    case E3D_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+const char* e3d_last_cuda_error(void) { return g_last_cuda_error.c_str(); }
+
+int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
+  if (!out || !p) return E3D_ERR_INPUT;
+  *out = nullptr;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->nphase < 1 || p->max_iter < 0) return E3D_ERR_INPUT;
+  if ((long long)p->nx * p->ny * p->nz > (1LL << 40)) return E3D_ERR_INPUT;
+  if (p->precision != E3D_PREC_FP64 && p->precision != E3D_PREC_MIXED) return E3D_ERR_INPUT;
+  if (p->criterion != E3D_CRIT_REF && p->criterion != E3D_CRIT_PRECOND_REL) return E3D_ERR_INPUT;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  if (p->device < 0 || p->device >= ndev) return E3D_ERR_INPUT;
+  e3d_handle* h = new e3d_handle();
+  h->prob = *p;
+  h->device = p->device;
+  auto fail = [&](int32_t rc) {
+    e3d_destroy(h);
+    return rc;
+  };
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "cudaSetDevice"));
+  cudaDeviceProp prop{};
+  if ((e = cudaGetDeviceProperties(&prop, h->device)) != cudaSuccess) return fail(cuda_fail(e, "props"));
+  h->num_sms = prop.multiProcessorCount;
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(cuda_fail(e, "cudaStreamCreate"));
+  h->G = make_dims(p->nx, p->ny, p->nz, h->num_sms);
+  const long long ns = h->G.ns, n3 = 3 * ns;
+  const int np = p->nphase;
+  // PCG grid: as many co-resident tile blocks as the device holds.
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel, NT, 0)) != cudaSuccess)
+    return fail(cuda_fail(e, "occupancy"));
+  if (per_sm < 1) return fail(E3D_ERR_CUDA);
+  h->pcg_grid = per_sm * h->num_sms;
+  h->partial_n = std::max(h->pcg_grid, h->num_sms * 4) * 12;
+  const long long halo = h->G.ntiles * h->G.tz;
+  int32_t rc = E3D_OK;
+  if ((rc = dalloc(h, &h->pix, ns)) || (rc = dalloc(h, &h->rod, 3 * (size_t)std::max(np - 1, 1))) ||
+      (rc = dalloc(h, &h->cmod, 36 * (size_t)np)) || (rc = dalloc(h, &h->cs, kCsStride * (size_t)np)) ||
+      (rc = dalloc(h, &h->cs32, kCsStride * (size_t)np)) || (rc = dalloc(h, &h->dk, 576 * (size_t)np)) ||
+      (rc = dalloc(h, &h->dkd, 72 * (size_t)np)) || (rc = dalloc(h, &h->u, n3)) || (rc = dalloc(h, &h->g, n3)) ||
+      (rc = dalloc(h, &h->b, n3)) || (rc = dalloc(h, &h->z, n3)) || (rc = dalloc(h, &h->h0, n3)) ||
+      (rc = dalloc(h, &h->h1, n3)) || (rc = dalloc(h, &h->Ah, n3)) || (rc = dalloc(h, &h->minv, 6 * ns)) ||
+      (rc = dalloc(h, &h->hx, 3 * halo * TILE_Y)) || (rc = dalloc(h, &h->hy, 3 * halo * TILE_X)) ||
+      (rc = dalloc(h, &h->hd, 3 * halo)) || (rc = dalloc(h, &h->partial, (size_t)h->partial_n)) ||
+      (rc = dalloc(h, &h->scalars, 64)) ||
+      (rc = dalloc(h, &h->history, (size_t)std::max(p->max_iter, 1))) || (rc = dalloc(h, &h->st, 1)) ||
+      (rc = dalloc(h, &h->bar, 1)) || (rc = dalloc(h, &h->err, 1)))
+    return fail(rc);
+  if ((e = cudaMemsetAsync(h->err, 0, sizeof(int), h->stream)) != cudaSuccess) return fail(cuda_fail(e, "memset"));
+  if ((e = cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream)) != cudaSuccess)
+    return fail(cuda_fail(e, "memset"));
+  if ((e = cudaMemsetAsync(h->h0, 0, sizeof(double) * n3, h->stream)) != cudaSuccess)
+    return fail(cuda_fail(e, "memset"));
+  if ((e = cudaMemsetAsync(h->h1, 0, sizeof(double) * n3, h->stream)) != cudaSuccess)
+    return fail(cuda_fail(e, "memset"));
+  if ((e = cudaMemsetAsync(h->u, 0, sizeof(double) * n3, h->stream)) != cudaSuccess)
+    return fail(cuda_fail(e, "memset"));
+  const double* s = p->strain;  // exx eyy ezz exz eyz exy
+  const double E[3][3] = {{s[0], s[5], s[3]}, {s[5], s[1], s[4]}, {s[3], s[4], s[2]}};
+  std::memcpy(h->J.E, E, sizeof E);
+  if ((rc = sync(h))) return fail(rc);
+  *out = h;
+  return E3D_OK;
+}
+
+int32_t e3d_destroy(e3d_handle_t* h) {
+  if (!h) return E3D_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* q : h->allocs) cudaFree(q);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return E3D_OK;
+}
+
+int64_t e3d_device_bytes(const e3d_handle_t* h) { return h ? h->bytes : 0; }
+int64_t e3d_launch_count(const e3d_handle_t* h) { return h ? h->launches : 0; }
+
+int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
+  if (!h || !pix) return E3D_ERR_INPUT;
+  const auto& p = h->prob;
+  if (p.flag_m == 1 && p.nphase > 1 && !rod) return E3D_ERR_INPUT;
+  const long long ns = h->G.ns;
+  // phase range check (ppixel_hdf5, src/elas3dxtal_pcg.f90:2986-2989) and
+  // conversion to 0-based ids.
+  std::vector<int32_t> p0((size_t)ns);
+  for (long long m = 0; m < ns; ++m) {
+    const int32_t v = pix[m];
+    if (v < 1 || v > p.nphase) return E3D_ERR_INPUT;
+    p0[(size_t)m] = v - 1;
+  }
+  cudaSetDevice(h->device);
+  E3D_CUDA(cudaMemcpyAsync(h->pix, p0.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, h->stream));
+  if (rod && p.nphase > 1)
+    E3D_CUDA(cudaMemcpyAsync(h->rod, rod, sizeof(double) * 3 * (p.nphase - 1), cudaMemcpyHostToDevice, h->stream));
+  else
+    E3D_CUDA(cudaMemsetAsync(h->rod, 0, sizeof(double) * 3, h->stream));
+  int32_t rc = sync(h);
+  if (rc) return rc;
+  h->uploaded = true;
+  h->femat_done = h->energy_done = h->solve_ready = h->minv_ready = false;
+  return E3D_OK;
+}
+
+int32_t e3d_femat(e3d_handle_t* h) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->uploaded) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const auto& p = h->prob;
+  FematParams P{};
+  P.nphase = p.nphase;
+  P.flag_m = p.flag_m;
+  P.c11 = p.c11;
+  P.c12 = p.c12;
+  P.c44 = p.c44;
+  // inclusion K, G from E1, nu1 (src/elas3dxtal_pcg.f90:314-316)
+  P.K1 = p.e1 / 3.0 / (1.0 - 2.0 * p.nu1);
+  P.G1 = p.e1 / 2.0 / (1.0 + p.nu1);
+  // isotropic matrix from C11/C12/C44 via E0, nu0 (:108-111, :305-312)
+  {
+    const double K0 = (p.c11 + 2.0 * p.c12) / 3.0;
+    const double G0 = (p.c11 - p.c12 + 3.0 * p.c44) / 5.0;
+    const double E0 = 9.0 * K0 * G0 / (3.0 * K0 + G0);
+    const double nu0 = (3.0 * K0 - 2.0 * G0) / (2.0 * (3.0 * K0 + G0));
+    P.Km = E0 / 3.0 / (1.0 - 2.0 * nu0);
+    P.Gm = E0 / 2.0 / (1.0 + nu0);
+  }
+  femat_phase_kernel<<<p.nphase, 32, 0, h->stream>>>(P, h->rod, h->cmod, h->cs, h->cs32, h->dk, h->dkd);
+  E3D_LAUNCHED(h);
+  femat_b_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->J, h->pix, h->dk, h->b);
+  E3D_LAUNCHED(h);
+  const int grid = reduction_grid(h);
+  femat_c_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->J, h->pix, h->dk, h->partial);
+  E3D_LAUNCHED(h);
+  double C = 0.0;
+  int32_t rc = reduce_to_host(h, grid, 1, 1, &C);
+  if (rc) return rc;
+  h->C = C;
+  h->femat_done = true;
+  h->energy_done = h->solve_ready = h->minv_ready = false;
+  return E3D_OK;
+}
+
+int32_t e3d_init_affine(e3d_handle_t* h) {
+  if (!h) return E3D_ERR_INPUT;
+  cudaSetDevice(h->device);
+  affine_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->J, h->u);
+  E3D_LAUNCHED(h);
+  h->energy_done = h->solve_ready = false;
+  return sync(h);
+}
+
+int32_t e3d_energy(e3d_handle_t* h, double* utot, double* gg) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  int32_t rc = launch_apply_tiles(h, h->u, h->Ah);
+  if (rc) return rc;
+  const int grid = reduction_grid(h) / 2 > 0 ? std::min(reduction_grid(h), h->partial_n / 2) : 1;
+  energy_finish_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->Ah, h->hx, h->hy, h->hd, h->u, h->b, h->g,
+                                                    h->partial);
+  E3D_LAUNCHED(h);
+  double out[2] = {0.0, 0.0};
+  rc = reduce_to_host(h, grid, 2, 2, out);
+  if (rc) return rc;
+  if (utot) *utot = h->C + out[0];
+  if (gg) *gg = out[1];
+  h->gg0 = out[1];
+  h->energy_done = true;
+  h->solve_ready = false;
+  return E3D_OK;
+}
+
+int32_t e3d_solve_begin(e3d_handle_t* h) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->energy_done) return E3D_ERR_STATE;
+  if (h->prob.precision != E3D_PREC_FP64) return E3D_ERR_INPUT;
+  cudaSetDevice(h->device);
+  cudaEvent_t e0, e1;
+  E3D_CUDA(cudaEventCreate(&e0));
+  E3D_CUDA(cudaEventCreate(&e1));
+  E3D_CUDA(cudaEventRecord(e0, h->stream));
+  // block-Jacobi (kkk == 1, src/elas3dxtal_pcg.f90:1498-1520)
+  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->pix, h->dkd, h->minv, nullptr);
+  E3D_LAUNCHED(h);
+  const int grid = reduction_grid(h);
+  pcg_init_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->minv, h->g, h->z, h->partial);
+  E3D_LAUNCHED(h);
+  pcg_init_scalars_kernel<<<1, 256, 0, h->stream>>>(h->partial, grid, h->gg0, h->prob.criterion, h->prob.tol,
+                                                    h->prob.max_iter, h->prob.divergence_reset, h->st);
+  E3D_LAUNCHED(h);
+  E3D_CUDA(cudaEventRecord(e1, h->stream));
+  int32_t rc = sync(h);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  h->ms_setup = ms;
+  h->ms_iter = 0.0;
+  h->minv_ready = true;
+  h->solve_ready = true;
+  return E3D_OK;
+}
+
+static int32_t fill_stats(e3d_handle* h, e3d_solve_stats_t* st, int32_t* exit_reason) {
+  PcgState S{};
+  E3D_CUDA(cudaMemcpy(&S, h->st, sizeof S, cudaMemcpyDeviceToHost));
+  int32_t reason = E3D_EXIT_RUNNING;
+  switch (S.status) {
+    case PCG_CONVERGED: reason = E3D_EXIT_CONVERGED; break;
+    case PCG_HAH: reason = E3D_EXIT_HAH_GUARD; break;
+    case PCG_MAXITER: reason = E3D_EXIT_MAXITER; break;
+    case PCG_BREAKDOWN: reason = E3D_EXIT_BREAKDOWN; break;
+    case PCG_TIMEOUT: reason = E3D_EXIT_TIMEOUT; break;
+    default: reason = E3D_EXIT_RUNNING;
+  }
+  *exit_reason = reason;
+  if (st) {
+    std::memset(st, 0, sizeof *st);
+    st->iterations = S.it;
+    st->exit_reason = reason;
+    st->resets = S.resets;
+    st->refinements = 0;
+    st->gg = S.gg;
+    st->gg0 = S.gg0;
+    st->rel_res = S.rel_res;
+    st->true_rel = NAN;
+    st->ms_setup = h->ms_setup;
+    st->ms_iter = h->ms_iter;
+  }
+  return E3D_OK;
+}
+
+int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
+  if (!h || n < 0) return E3D_ERR_INPUT;
+  if (!h->solve_ready) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  PcgArgs P{};
+  P.A = apply_args(h, nullptr, h->Ah);
+  P.h0 = h->h0;
+  P.h1 = h->h1;
+  P.u = h->u;
+  P.g = h->g;
+  P.z = h->z;
+  P.Ah = h->Ah;
+  P.minv = h->minv;
+  P.partA = h->partial;
+  P.partB = h->partial + h->pcg_grid;
+  P.st = h->st;
+  P.history = h->history;
+  P.bar = h->bar;
+  P.err = h->err;
+  P.timeout_ns = 60ull * 1000000000ull;
+  E3D_CUDA(cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream));
+  cudaEvent_t e0, e1;
+  E3D_CUDA(cudaEventCreate(&e0));
+  E3D_CUDA(cudaEventCreate(&e1));
+  E3D_CUDA(cudaEventRecord(e0, h->stream));
+  // Chunks of iterations per cooperative launch keep single launches short.
+  int remaining = n;
+  int32_t rc = E3D_OK;
+  while (remaining > 0) {
+    const int chunk = std::min(remaining, 256);
+    P.it_limit = chunk;
+    void* args[] = {&P};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)pcg_persistent_kernel, dim3(h->pcg_grid), dim3(NT),
+                                                args, 0, h->stream);
+    h->launches++;
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "cudaLaunchCooperativeKernel(pcg)");
+      break;
+    }
+    remaining -= chunk;
+    if (remaining > 0) {
+      PcgState S{};
+      e = cudaMemcpyAsync(&S, h->st, sizeof S, cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(e, "pcg state");
+        break;
+      }
+      if (S.status != PCG_RUNNING) break;
+    }
+  }
+  cudaEventRecord(e1, h->stream);
+  int32_t rs = sync(h);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  h->ms_iter += ms;
+  int32_t reason = 0;
+  int32_t rf = fill_stats(h, st, &reason);
+  if (rf) return rf;
+  if (rs == E3D_ERR_TIMEOUT || reason == E3D_EXIT_TIMEOUT) return E3D_ERR_TIMEOUT;
+  if (rs) return rs;
+  if (reason == E3D_EXIT_BREAKDOWN) return E3D_ERR_BREAKDOWN;
+  return E3D_OK;
+}
+
+int32_t e3d_solve(e3d_handle_t* h, e3d_solve_stats_t* st) {
+  int32_t rc = e3d_solve_begin(h);
+  if (rc) return rc;
+  e3d_solve_stats_t local{};
+  rc = e3d_iterate(h, h->prob.max_iter, &local);
+  if (st) *st = local;
+  if (rc) return rc;
+  h->energy_done = false;  // g is now the recurrence residual; energy recomputes it
+  if (local.exit_reason == E3D_EXIT_MAXITER) return E3D_ERR_MAXITER;
+  return E3D_OK;
+}
+
+int32_t e3d_stress(e3d_handle_t* h, double strav[6], double epsav[6]) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const int grid = std::max(1, std::min(reduction_grid(h), h->partial_n / 12));
+  stress_avg_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->J, h->pix, h->cmod, h->prob.nphase, h->u, h->partial);
+  E3D_LAUNCHED(h);
+  double out[12];
+  int32_t rc = reduce_to_host(h, grid, 12, 12, out);
+  if (rc) return rc;
+  const double ns = (double)h->G.ns;
+  for (int r = 0; r < 6; ++r) {
+    if (strav) strav[r] = out[r] / ns;
+    if (epsav) epsav[r] = out[6 + r] / ns;
+  }
+  return E3D_OK;
+}
+
+int32_t e3d_stress_field(e3d_handle_t* h, double* sigma, double* vm) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const long long ns = h->G.ns;
+  // sigma lands in z/h1 scratch (6*ns fits in z + half of h1? use Ah + z)
+  double* dsig = nullptr;
+  double* dvm = nullptr;
+  int32_t rc = E3D_OK;
+  if ((rc = dalloc(h, &dsig, 6 * (size_t)ns)) || (rc = dalloc(h, &dvm, (size_t)ns))) return rc;
+  stress_field_kernel<<<blocks_for(ns, 256), 256, 0, h->stream>>>(h->G, h->J, h->pix, h->cmod, h->prob.nphase,
+                                                                   h->u, dsig, dvm);
+  E3D_LAUNCHED(h);
+  if (sigma) E3D_CUDA(cudaMemcpyAsync(sigma, dsig, sizeof(double) * 6 * ns, cudaMemcpyDeviceToHost, h->stream));
+  if (vm) E3D_CUDA(cudaMemcpyAsync(vm, dvm, sizeof(double) * ns, cudaMemcpyDeviceToHost, h->stream));
+  rc = sync(h);
+  // release the temporaries
+  for (void* q : {(void*)dsig, (void*)dvm}) {
+    for (size_t i = 0; i < h->allocs.size(); ++i)
+      if (h->allocs[i] == q) {
+        h->allocs.erase(h->allocs.begin() + (long)i);
+        break;
+      }
+    cudaFree(q);
+  }
+  h->bytes -= (int64_t)(sizeof(double) * 7 * ns + 32);
+  return rc;
+}
+
+int32_t e3d_run(e3d_handle_t* h, double utot[2], double out12[12], e3d_solve_stats_t* st) {
+  if (!h) return E3D_ERR_INPUT;
+  int32_t rc;
+  if ((rc = e3d_femat(h))) return rc;
+  if ((rc = e3d_init_affine(h))) return rc;
+  double u0 = 0.0, gg0 = 0.0;
+  if ((rc = e3d_energy(h, &u0, &gg0))) return rc;
+  e3d_solve_stats_t local{};
+  int32_t rs = e3d_solve(h, &local);
+  if (st) *st = local;
+  if (rs != E3D_OK && rs != E3D_ERR_MAXITER) return rs;
+  double u1 = 0.0, gg = 0.0;
+  if ((rc = e3d_energy(h, &u1, &gg))) return rc;
+  if (st) st->true_rel = std::sqrt(gg / gg0);
+  if (utot) {
+    utot[0] = u0;
+    utot[1] = u1;
+  }
+  if ((rc = e3d_stress(h, out12 ? out12 : nullptr, out12 ? out12 + 6 : nullptr))) return rc;
+  return rs;
+}
+
+int32_t e3d_apply(e3d_handle_t* h, const double* x, double* y) {
+  if (!h || !x || !y) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const long long n3 = 3 * h->G.ns;
+  // stage through z (input) and h1 (output); both are solver scratch
+  E3D_CUDA(cudaMemcpyAsync(h->z, x, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  int32_t rc = apply_device(h, h->z, h->h1);
+  if (rc) return rc;
+  E3D_CUDA(cudaMemcpyAsync(y, h->h1, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
+  h->solve_ready = false;
+  return sync(h);
+}
+
+int32_t e3d_apply_device(e3d_handle_t* h, const double* d_x, double* d_y) {
+  if (!h || !d_x || !d_y) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  int32_t rc = apply_device(h, d_x, d_y);
+  if (rc) return rc;
+  return sync(h);
+}
+
+int32_t e3d_set_u(e3d_handle_t* h, const double* u) {
+  if (!h || !u) return E3D_ERR_INPUT;
+  cudaSetDevice(h->device);
+  E3D_CUDA(cudaMemcpyAsync(h->u, u, sizeof(double) * 3 * h->G.ns, cudaMemcpyHostToDevice, h->stream));
+  h->energy_done = h->solve_ready = false;
+  return sync(h);
+}
+
+static int32_t get_vec(e3d_handle_t* h, const double* d, double* out, size_t count) {
+  if (!h || !out) return E3D_ERR_INPUT;
+  cudaSetDevice(h->device);
+  E3D_CUDA(cudaMemcpyAsync(out, d, sizeof(double) * count, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int32_t e3d_get_u(e3d_handle_t* h, double* u) { return h ? get_vec(h, h->u, u, 3 * h->G.ns) : E3D_ERR_INPUT; }
+int32_t e3d_get_g(e3d_handle_t* h, double* g) { return h ? get_vec(h, h->g, g, 3 * h->G.ns) : E3D_ERR_INPUT; }
+int32_t e3d_get_b(e3d_handle_t* h, double* b) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  return get_vec(h, h->b, b, 3 * h->G.ns);
+}
+
+int32_t e3d_get_C(e3d_handle_t* h, double* C) {
+  if (!h || !C) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  *C = h->C;
+  return E3D_OK;
+}
+
+int32_t e3d_get_cmod(e3d_handle_t* h, double* cmod) {
+  if (!h) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  return get_vec(h, h->cmod, cmod, 36 * (size_t)h->prob.nphase);
+}
+
+int32_t e3d_get_dk(e3d_handle_t* h, double* dk) {
+  if (!h || !dk) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  const int np = h->prob.nphase;
+  std::vector<double> t((size_t)576 * np);
+  int32_t rc = get_vec(h, h->dk, t.data(), t.size());
+  if (rc) return rc;
+  // device [p][a][i][b][j] -> Fortran dk(nphase,8,3,8,3)
+  for (int p = 0; p < np; ++p)
+    for (int a = 0; a < 8; ++a)
+      for (int i = 0; i < 3; ++i)
+        for (int b = 0; b < 8; ++b)
+          for (int j = 0; j < 3; ++j)
+            dk[(size_t)p + (size_t)np * (a + 8 * (i + 3 * (b + 8 * j)))] =
+                t[(size_t)p * 576 + (a * 3 + i) * 24 + b * 3 + j];
+  return E3D_OK;
+}
+
+int32_t e3d_get_minv(e3d_handle_t* h, double* minv) {
+  if (!h || !minv) return E3D_ERR_INPUT;
+  if (!h->minv_ready) return E3D_ERR_STATE;
+  const long long ns = h->G.ns;
+  std::vector<double> t((size_t)6 * ns);
+  int32_t rc = get_vec(h, h->minv, t.data(), t.size());
+  if (rc) return rc;
+  // 6 symmetric planes (00 11 22 01 02 12) -> M_block_inv(ns,3,3)
+  const int map[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      std::memcpy(minv + (size_t)ns * (i + 3 * j), t.data() + (size_t)ns * map[i][j], sizeof(double) * ns);
+  return E3D_OK;
+}
+
+int32_t e3d_get_history(e3d_handle_t* h, double* hist, int32_t n, int32_t* count) {
+  if (!h || n < 0) return E3D_ERR_INPUT;
+  PcgState S{};
+  cudaSetDevice(h->device);
+  E3D_CUDA(cudaMemcpy(&S, h->st, sizeof S, cudaMemcpyDeviceToHost));
+  const int c = std::max(0, std::min(n, S.it));
+  if (c > 0 && hist) E3D_CUDA(cudaMemcpy(hist, h->history, sizeof(double) * c, cudaMemcpyDeviceToHost));
+  if (count) *count = c;
+  return E3D_OK;
+}
+
+int32_t e3d_device_ptrs(e3d_handle_t* h, double** d_u, double** d_g, double** d_b) {
+  if (!h) return E3D_ERR_INPUT;
+  if (d_u) *d_u = h->u;
+  if (d_g) *d_g = h->g;
+  if (d_b) *d_b = h->b;
+  return E3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1030 @@
+// Kernels of the sm_103a voxel-FE solver.  See e3d_device.cuh for the element
+// arithmetic.  Layout in HBM (all component-major, node m = x + nx*(y + ny*z)):
+//   u, g, b, z, h[2], Ah : 3*ns values each
+//   minv                 : 6*ns (symmetric 3x3 block inverse: 00 11 22 01 02 12)
+//   pix                  : ns int32, 0-based phase
+//   cs                   : nphase*108 scaled stiffness (C/16, C/48, C/144)
+//   dk                   : nphase*576, [p][a][i][b][j] (reference local order)
+//   dkd                  : nphase*72 diagonal 3x3 blocks [p][a][i][j]
+//   hx, hy, hd           : tile-edge force halos (see apply_tile)
+#pragma once
+#include <cstdint>
+
+#include "e3d_device.cuh"
+
+namespace e3d {
+
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 8;
+constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
+
+// Device status codes (host maps them to E3D_*).
+enum : int { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_BAD_INDEX = 2 };
+// PCG status.
+enum : int { PCG_RUNNING = 0, PCG_CONVERGED = 1, PCG_HAH = 2, PCG_MAXITER = 3, PCG_BREAKDOWN = 4, PCG_TIMEOUT = 5 };
+
+struct GridDims {
+  int nx, ny, nz;
+  long long ns;
+  int ntx, nty, ntz;  // tiles per direction
+  int tz;             // element planes per tile
+  long long ntiles;
+};
+
+__host__ __device__ inline int wrapi(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
+template <typename T>
+struct ApplyArgs {
+  GridDims g;
+  const int32_t* __restrict__ pix;  // 0-based phase per voxel
+  const T* __restrict__ cs;         // scaled stiffness table
+  const T* __restrict__ x;          // input (or h_old when fused)
+  const T* __restrict__ zv;         // z (fused Fletcher-Reeves update only)
+  T gamma;                          // FR coefficient
+  int reset;                        // 1: h_new = z
+  T* __restrict__ hnew;             // fused: h_new written for owned nodes
+  T* __restrict__ y;                // in-tile part of K x
+  T* __restrict__ hx;               // [3][ntiles][tz][TILE_Y]
+  T* __restrict__ hy;               // [3][ntiles][tz][TILE_X]
+  T* __restrict__ hd;               // [3][ntiles][tz]
+};
+
+template <typename T>
+struct ApplySmem {
+  T node[2][3][(TILE_X + 1) * (TILE_Y + 1)];
+  T r[9][NT];
+};
+
+// One tile: TILE_X x TILE_Y element columns marching through tz element planes
+// (plus one redundant plane below).  Each thread owns node column (x0+tx,
+// y0+ty) and the element whose lower corner it is.  Element forces are summed
+// into the nodes inside the tile through shared memory; the contributions to
+// the nodes just past the tile's high-x / high-y edges go to the halo buffers
+// and are added by the consumer (apply_finish / the PCG update), which keeps
+// every sum in a fixed order.  FUSED: the input is h_new = z + gamma*h_old (or
+// z on reset) formed on load -- the Fletcher-Reeves update of the previous
+// iteration (src/elas3dxtal_pcg.f90:1988-1995) folded into this pass -- and
+// h_new is stored for the tile's own nodes.  Returns this thread's share of
+// h_new . (K h_new) through hAh.
+template <typename T, bool FUSED>
+__device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& sm, double& hAh) {
+  const GridDims& G = A.g;
+  const int tid = threadIdx.x;
+  const int tx = tid % TILE_X, ty = tid / TILE_X;
+  const int tix = (int)(tile % G.ntx);
+  const int tiy = (int)((tile / G.ntx) % G.nty);
+  const int tiz = (int)(tile / ((long long)G.ntx * G.nty));
+  const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+  const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+  const bool active = (tx < wx) && (ty < wy);
+  const int xg = x0 + tx, yg = y0 + ty;
+  const long long ns = G.ns;
+  const long long nxy = (long long)G.nx * G.ny;
+  const int nhalo = wx + wy + 1;
+  // halo node (lx, ly) for loader thread q = tid < nhalo
+  int hlx = 0, hly = 0;
+  if (tid < wy) {
+    hlx = wx;
+    hly = tid;
+  } else if (tid < wy + wx) {
+    hlx = tid - wy;
+    hly = wy;
+  } else {
+    hlx = wx;
+    hly = wy;
+  }
+  const int hgx = wrapi(x0 + hlx, G.nx), hgy = wrapi(y0 + hly, G.ny);
+
+  auto fetch = [&](long long m, T (&v)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (FUSED) {
+        const T zz = __ldcg(A.zv + m + c * ns);
+        v[c] = A.reset ? zz : fma_(A.gamma, __ldcg(A.x + m + c * ns), zz);
+      } else {
+        v[c] = __ldcg(A.x + m + c * ns);
+      }
+    }
+  };
+  auto load_plane = [&](int zl, bool own) {
+    const int zp = wrapi(zl, G.nz);
+    T* buf0 = sm.node[(zl + 2) & 1][0];
+    const int stride = (TILE_X + 1) * (TILE_Y + 1);
+    if (active) {
+      const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
+      T v[3];
+      fetch(m, v);
+      if (FUSED && own) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = v[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) buf0[c * stride + ty * (TILE_X + 1) + tx] = v[c];
+    }
+    if (tid < nhalo) {
+      const long long m = (long long)hgx + (long long)G.nx * hgy + nxy * zp;
+      T v[3];
+      fetch(m, v);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) buf0[c * stride + hly * (TILE_X + 1) + hlx] = v[c];
+    }
+  };
+  auto read_corners = [&](int zl, T (&v)[3][4]) {
+    const T* buf0 = sm.node[(zl + 2) & 1][0];
+    const int stride = (TILE_X + 1) * (TILE_Y + 1);
+    const int o = ty * (TILE_X + 1) + tx;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v[c][0] = buf0[c * stride + o];
+      v[c][1] = buf0[c * stride + o + 1];
+      v[c][2] = buf0[c * stride + o + TILE_X + 1];
+      v[c][3] = buf0[c * stride + o + TILE_X + 2];
+    }
+  };
+
+  T cur[3][4], Pold[3][4], carry[3][4];
+  load_plane(z0 - 1, false);
+  __syncthreads();
+  if (active) {
+    read_corners(z0 - 1, cur);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) had_xy(cur[c], Pold[c]);
+  }
+  const int htiles_stride = G.tz;  // per-tile plane stride in halo buffers
+  for (int k = z0 - 1; k < z0 + wz; ++k) {
+    const bool own_next = (k + 1 >= z0) && (k + 1 < z0 + wz);
+    load_plane(k + 1, own_next);
+    __syncthreads();
+    T rr[3][4];
+    T nxt[3][4];
+    if (active) {
+      read_corners(k + 1, nxt);
+      T Pn[3][4];
+      T h[3][8];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        had_xy(nxt[c], Pn[c]);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          h[c][b] = Pn[c][b] + Pold[c][b];
+          h[c][b + 4] = Pn[c][b] - Pold[c][b];
+        }
+      }
+      const int zp = wrapi(k, G.nz);
+      const int ph = __ldg(A.pix + (long long)xg + (long long)G.nx * yg + nxy * zp);
+      T f[3][8];
+      element_modal<T>(A.cs + (long long)ph * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        T lo[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          lo[b] = f[c][b] - f[c][b + 4];
+          const T hi = f[c][b] + f[c][b + 4];
+          if (k >= z0) lo[b] += carry[c][b];
+          carry[c][b] = hi;
+        }
+        if (k >= z0) had_xy_adj(lo, rr[c]);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+      }
+    }
+    if (k >= z0) {
+      if (active) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          sm.r[3 * c + 0][tid] = rr[c][1];  // to node (x+1, y)
+          sm.r[3 * c + 1][tid] = rr[c][2];  // to node (x, y+1)
+          sm.r[3 * c + 2][tid] = rr[c][3];  // to node (x+1, y+1)
+        }
+      }
+      __syncthreads();
+      if (active) {
+        const int lz = k - z0;
+        const long long m = (long long)xg + (long long)G.nx * yg + nxy * wrapi(k, G.nz);
+        T hxv[3], hyv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          T acc = rr[c][0];
+          if (tx > 0) acc += sm.r[3 * c + 0][tid - 1];
+          if (ty > 0) acc += sm.r[3 * c + 1][tid - TILE_X];
+          if (tx > 0 && ty > 0) acc += sm.r[3 * c + 2][tid - TILE_X - 1];
+          A.y[m + c * ns] = acc;
+          hAh += (double)cur[c][0] * (double)acc;
+          hxv[c] = rr[c][1] + (ty > 0 ? sm.r[3 * c + 2][tid - TILE_X] : T(0));
+          hyv[c] = rr[c][2] + (tx > 0 ? sm.r[3 * c + 2][tid - 1] : T(0));
+        }
+        const long long hb = tile * htiles_stride + lz;
+        if (tx == wx - 1) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            A.hx[((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty] = hxv[c];
+            hAh += (double)cur[c][1] * (double)hxv[c];
+          }
+        }
+        if (ty == wy - 1) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            A.hy[((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx] = hyv[c];
+            hAh += (double)cur[c][2] * (double)hyv[c];
+          }
+        }
+        if (tx == wx - 1 && ty == wy - 1) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            A.hd[(long long)c * G.ntiles * htiles_stride + hb] = rr[c][3];
+            hAh += (double)cur[c][3] * (double)rr[c][3];
+          }
+        }
+      }
+    }
+    if (active) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cur[c][b] = nxt[c][b];
+    }
+  }
+}
+
+// Halo contribution for node (x, y, z) from the neighbouring tiles.
+template <typename T>
+__device__ __forceinline__ void halo_add(const GridDims& G, const T* __restrict__ hx,
+                                         const T* __restrict__ hy, const T* __restrict__ hd,
+                                         int x, int y, int z, T (&v)[3]) {
+  const int tix = x / TILE_X, lx = x - tix * TILE_X;
+  const int tiy = y / TILE_Y, ly = y - tiy * TILE_Y;
+  const int tiz = z / G.tz, lz = z - tiz * G.tz;
+  if (lx != 0 && ly != 0) return;
+  const int txl = tix == 0 ? G.ntx - 1 : tix - 1;
+  const int tyd = tiy == 0 ? G.nty - 1 : tiy - 1;
+  const long long plane = (long long)tiz * G.nty;
+  const long long per_c = G.ntiles * G.tz;
+  if (lx == 0) {
+    const long long t = (long long)txl + (long long)G.ntx * (tiy + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + (c * per_c + t * G.tz + lz) * TILE_Y + ly);
+  }
+  if (ly == 0) {
+    const long long t = (long long)tix + (long long)G.ntx * (tyd + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + (c * per_c + t * G.tz + lz) * TILE_X + lx);
+  }
+  if (lx == 0 && ly == 0) {
+    const long long t = (long long)txl + (long long)G.ntx * (tyd + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + c * per_c + t * G.tz + lz);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stand-alone apply: one tile per block, then apply_finish adds the halos.
+template <typename T>
+__global__ void __launch_bounds__(NT, 1) apply_tiles_kernel(ApplyArgs<T> A, double* partial) {
+  __shared__ ApplySmem<T> sm;
+  __shared__ double red[NT / 32];
+  double hAh = 0.0;
+  apply_tile<T, false>(A, blockIdx.x, sm, hAh);
+  const double s = block_sum<NT>(hAh, red);
+  if (partial && threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void apply_finish_kernel(GridDims G, const T* __restrict__ yin, const T* __restrict__ hx,
+                                    const T* __restrict__ hy, const T* __restrict__ hd,
+                                    T* __restrict__ yout) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= G.ns) return;
+  const int x = (int)(m % G.nx);
+  const int y = (int)((m / G.nx) % G.ny);
+  const int z = (int)(m / ((long long)G.nx * G.ny));
+  T v[3] = {yin[m], yin[m + G.ns], yin[m + 2 * G.ns]};
+  halo_add<T>(G, hx, hy, hd, x, y, z, v);
+  yout[m] = v[0];
+  yout[m + G.ns] = v[1];
+  yout[m + 2 * G.ns] = v[2];
+}
+
+// energy_OpenMP tail (src/elas3dxtal_pcg.f90:1332-1340): g = Ku + b,
+// partial sums of (u.Ku/2 + b.u) and of g.g (gg0, :452).
+__global__ void __launch_bounds__(256) energy_finish_kernel(GridDims G, const double* __restrict__ ku,
+                                                            const double* __restrict__ hx,
+                                                            const double* __restrict__ hy,
+                                                            const double* __restrict__ hd,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ b,
+                                                            double* __restrict__ g, double* partial) {
+  __shared__ double red[8];
+  double eu = 0.0, gg = 0.0;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
+       m += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(m % G.nx);
+    const int y = (int)((m / G.nx) % G.ny);
+    const int z = (int)(m / ((long long)G.nx * G.ny));
+    double v[3] = {ku[m], ku[m + G.ns], ku[m + 2 * G.ns]};
+    halo_add<double>(G, hx, hy, hd, x, y, z, v);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long i = m + c * G.ns;
+      eu += 0.5 * u[i] * v[c] + b[i] * u[i];
+      const double gv = v[c] + b[i];
+      g[i] = gv;
+      gg += gv * gv;
+    }
+  }
+  const double s1 = block_sum<256>(eu, red);
+  const double s2 = block_sum<256>(gg, red);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = s1;
+    partial[2 * blockIdx.x + 1] = s2;
+  }
+}
+
+// Sums n partials of stride `stride` in a fixed order (single block).
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int n, int stride,
+                                       int nfields, double* __restrict__ out) {
+  __shared__ double red[8];
+  for (int f = 0; f < nfields; ++f) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[(long long)i * stride + f];
+    const double t = block_sum<256>(s, red);
+    if (threadIdx.x == 0) out[f] = t;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// femat.  One block of 32 threads per phase.
+struct FematParams {
+  int nphase, flag_m;
+  double c11, c12, c44, K1, G1, Km, Gm;
+};
+
+// rotatestiffnessby (src/elas3dxtal_pcg.f90:2535-2633) for one grain.
+__device__ void bond_rotate(const double r[3], double c11, double c12, double c44, double out[6][6]) {
+  double Cc[6][6];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) Cc[i][j] = 0.0;
+  Cc[0][0] = Cc[1][1] = Cc[2][2] = c11;
+  Cc[0][1] = Cc[0][2] = Cc[1][2] = Cc[1][0] = Cc[2][0] = Cc[2][1] = c12;
+  Cc[3][3] = Cc[4][4] = Cc[5][5] = c44;
+  const double rdotr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  const double term1 = 1.0 - rdotr;
+  double term2 = 1.0 + rdotr;
+  double Q[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Q[i][j] = (i == j ? term1 : 0.0) + 2.0 * r[i] * r[j];
+  Q[0][1] -= 2.0 * r[2];
+  Q[0][2] += 2.0 * r[1];
+  Q[1][2] -= 2.0 * r[0];
+  Q[1][0] += 2.0 * r[2];
+  Q[2][0] -= 2.0 * r[1];
+  Q[2][1] += 2.0 * r[0];
+  if (term2 > 1.0e-12) {
+    term2 = 1.0 / term2;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Q[i][j] *= term2;
+  } else {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Q[i][j] = (i == j) ? 1.0 : 0.0;
+  }
+  double N[6][6];
+  for (int row = 0; row < 3; ++row) {
+    N[row][0] = Q[row][0] * Q[row][0];
+    N[row][1] = Q[row][1] * Q[row][1];
+    N[row][2] = Q[row][2] * Q[row][2];
+    N[row][3] = Q[row][1] * Q[row][2];
+    N[row][4] = Q[row][2] * Q[row][0];
+    N[row][5] = Q[row][0] * Q[row][1];
+  }
+  N[3][0] = 2.0 * Q[2][0] * Q[0][0];
+  N[3][1] = 2.0 * Q[2][1] * Q[0][1];
+  N[3][2] = 2.0 * Q[2][2] * Q[0][2];
+  N[3][3] = Q[0][1] * Q[2][2] + Q[0][2] * Q[2][1];
+  N[3][4] = Q[0][2] * Q[2][0] + Q[0][0] * Q[2][2];
+  N[3][5] = Q[0][0] * Q[2][1] + Q[0][1] * Q[2][0];
+  N[4][0] = 2.0 * Q[1][0] * Q[2][0];
+  N[4][1] = 2.0 * Q[1][1] * Q[2][1];
+  N[4][2] = 2.0 * Q[1][2] * Q[2][2];
+  N[4][3] = Q[1][1] * Q[2][2] + Q[1][2] * Q[2][1];
+  N[4][4] = Q[1][0] * Q[2][2] + Q[1][2] * Q[2][0];
+  N[4][5] = Q[1][1] * Q[2][0] + Q[1][0] * Q[2][1];
+  N[5][0] = 2.0 * Q[0][0] * Q[1][0];
+  N[5][1] = 2.0 * Q[0][1] * Q[1][1];
+  N[5][2] = 2.0 * Q[0][2] * Q[1][2];
+  N[5][3] = Q[0][1] * Q[1][2] + Q[0][2] * Q[1][1];
+  N[5][4] = Q[0][2] * Q[1][0] + Q[0][0] * Q[1][2];
+  N[5][5] = Q[0][0] * Q[1][1] + Q[0][1] * Q[1][0];
+  double Tm[6][6];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += N[k][i] * Cc[k][j];
+      Tm[i][j] = s;
+    }
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += Tm[i][k] * N[k][j];
+      out[i][j] = s;
+    }
+}
+
+// Reference local node r (1..8 -> 0..7) to corner index a = ox + 2oy + 4oz.
+__constant__ int kRefToCorner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+
+__global__ void femat_phase_kernel(FematParams P, const double* __restrict__ rod, double* __restrict__ cmod,
+                                   double* __restrict__ cs, float* __restrict__ cs32,
+                                   double* __restrict__ dk, double* __restrict__ dkd) {
+  const int p = blockIdx.x;
+  __shared__ double csh[kCsStride];
+  __shared__ double col[24][24];  // col[c][r] = (K e_c)[r], c/r = refnode*3 + dof
+  if (threadIdx.x == 0) {
+    double C6[6][6];
+    const bool iso_phase = (p == P.nphase - 1) || (P.flag_m == 0);
+    if (iso_phase) {
+      // K*ck + G*cmu (src/elas3dxtal_pcg.f90:655-664, 680-682, 701-705)
+      const double K = (p == P.nphase - 1) ? P.K1 : P.Km;
+      const double Gs = (p == P.nphase - 1) ? P.G1 : P.Gm;
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+          const double ck = (i < 3 && j < 3) ? 1.0 : 0.0;
+          double cmu = 0.0;
+          if (i < 3 && j < 3) cmu = (i == j) ? 4.0 / 3.0 : -2.0 / 3.0;
+          if (i >= 3 && i == j) cmu = 1.0;
+          C6[i][j] = K * ck + Gs * cmu;
+        }
+    } else {
+      const double r[3] = {rod[3 * p], rod[3 * p + 1], rod[3 * p + 2]};
+      bond_rotate(r, P.c11, P.c12, P.c44, C6);
+    }
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) {
+        cmod[p + (long long)P.nphase * (i + 6 * j)] = C6[i][j];
+        csh[6 * i + j] = C6[i][j] / 16.0;
+        csh[36 + 6 * i + j] = C6[i][j] / 48.0;
+        csh[72 + 6 * i + j] = C6[i][j] / 144.0;
+      }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) {
+    cs[(long long)p * kCsStride + i] = csh[i];
+    cs32[(long long)p * kCsStride + i] = (float)csh[i];
+  }
+  // dk columns: K applied to unit nodal vectors with the same element routine
+  // as the stencil, so the preconditioner and b see exactly that matrix.
+  if (threadIdx.x < 24) {
+    const int cidx = threadIdx.x;
+    const int rb = cidx / 3, j = cidx % 3;
+    double u[3][8], r[3][8];
+    for (int c = 0; c < 3; ++c)
+      for (int a = 0; a < 8; ++a) u[c][a] = 0.0;
+    u[j][kRefToCorner[rb]] = 1.0;
+    element_apply<double>(csh, u, r);
+    for (int ra = 0; ra < 8; ++ra)
+      for (int i = 0; i < 3; ++i) col[cidx][ra * 3 + i] = r[i][kRefToCorner[ra]];
+  }
+  __syncthreads();
+  // symmetric dk: entry (r, c) taken from the column with the larger index
+  for (int e = threadIdx.x; e < 576; e += blockDim.x) {
+    const int r = e / 24, c = e % 24;
+    const double v = (r <= c) ? col[c][r] : col[r][c];
+    dk[(long long)p * 576 + e] = v;
+    const int ra = r / 3, i = r % 3, cb = c / 3, j = c % 3;
+    if (ra == cb) dkd[(long long)p * 72 + ra * 9 + i * 3 + j] = v;
+  }
+}
+
+// Periodic-jump force b (src/elas3dxtal_pcg.f90:815-1100), node-centric so
+// the sum over a node's boundary elements has a fixed order.  An element with
+// lower corner (i,j,k) on the high face of any direction d has nodal jumps
+// delta(a, :) = sum_d [wrap_d] [o_d(a)] E(:, d) n_d.
+struct JumpParams {
+  double E[3][3];  // symmetric strain tensor
+};
+
+__device__ __forceinline__ void element_delta(const GridDims& G, const JumpParams& J, int i, int j, int k,
+                                              double (&d)[8][3], bool& any) {
+  const bool wx = (i == G.nx - 1), wy = (j == G.ny - 1), wz = (k == G.nz - 1);
+  any = wx || wy || wz;
+  for (int ra = 0; ra < 8; ++ra) {
+    const int a = kRefToCorner[ra];
+    const int ox = a & 1, oy = (a >> 1) & 1, oz = (a >> 2) & 1;
+    for (int c = 0; c < 3; ++c) {
+      double v = 0.0;
+      if (wx && ox) v += J.E[c][0] * (double)G.nx;
+      if (wy && oy) v += J.E[c][1] * (double)G.ny;
+      if (wz && oz) v += J.E[c][2] * (double)G.nz;
+      d[ra][c] = v;
+    }
+  }
+}
+
+__global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+                               const double* __restrict__ dk, double* __restrict__ b) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= G.ns) return;
+  const int x = (int)(m % G.nx);
+  const int y = (int)((m / G.nx) % G.ny);
+  const int z = (int)(m / ((long long)G.nx * G.ny));
+  double acc[3] = {0.0, 0.0, 0.0};
+  const bool edge = (x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1);
+  if (edge) {
+    // elements containing m in reference order 27,7,6,5,25,15,14,13 (local node ra)
+    for (int ra = 0; ra < 8; ++ra) {
+      const int a = kRefToCorner[ra];
+      const int ex = wrapi(x - (a & 1), G.nx), ey = wrapi(y - ((a >> 1) & 1), G.ny),
+                ez = wrapi(z - ((a >> 2) & 1), G.nz);
+      double d[8][3];
+      bool any;
+      element_delta(G, J, ex, ey, ez, d, any);
+      if (!any) continue;
+      const int ph = pix[(long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez];
+      const double* D = dk + (long long)ph * 576;
+      for (int i = 0; i < 3; ++i) {
+        double s = 0.0;
+        for (int rb = 0; rb < 8; ++rb)
+          for (int jj = 0; jj < 3; ++jj) s += D[(ra * 3 + i) * 24 + rb * 3 + jj] * d[rb][jj];
+        acc[i] += s;
+      }
+    }
+  }
+  b[m] = acc[0];
+  b[m + G.ns] = acc[1];
+  b[m + 2 * G.ns] = acc[2];
+}
+
+// Constant C = 1/2 sum_e delta_e^T K_e delta_e over boundary elements.
+__global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+                                                      const double* __restrict__ dk, double* partial) {
+  __shared__ double red[8];
+  double acc = 0.0;
+  // boundary elements: enumerate the three high faces without double counting
+  const long long nfx = (long long)G.ny * G.nz;                        // i = nx-1
+  const long long nfy = (long long)(G.nx - 1) * G.nz;                  // j = ny-1, i < nx-1
+  const long long nfz = (long long)(G.nx - 1) * (G.ny - 1);            // k = nz-1, i < nx-1, j < ny-1
+  const long long total = nfx + nfy + nfz;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    if (t < nfx) {
+      i = G.nx - 1;
+      j = (int)(t % G.ny);
+      k = (int)(t / G.ny);
+    } else if (t < nfx + nfy) {
+      const long long s = t - nfx;
+      j = G.ny - 1;
+      i = (int)(s % (G.nx - 1));
+      k = (int)(s / (G.nx - 1));
+    } else {
+      const long long s = t - nfx - nfy;
+      k = G.nz - 1;
+      i = (int)(s % (G.nx - 1));
+      j = (int)(s / (G.nx - 1));
+    }
+    double d[8][3];
+    bool any;
+    element_delta(G, J, i, j, k, d, any);
+    const int ph = pix[(long long)i + (long long)G.nx * j + (long long)G.nx * G.ny * k];
+    const double* D = dk + (long long)ph * 576;
+    double e = 0.0;
+    for (int r = 0; r < 24; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < 24; ++c) s += D[r * 24 + c] * d[c / 3][c % 3];
+      e += d[r / 3][r % 3] * s;
+    }
+    acc += 0.5 * e;
+  }
+  const double s = block_sum<256>(acc, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Affine initial guess (src/elas3dxtal_pcg.f90:423-438).
+__global__ void affine_kernel(GridDims G, JumpParams J, double* __restrict__ u) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= G.ns) return;
+  const double x = (double)(m % G.nx);
+  const double y = (double)((m / G.nx) % G.ny);
+  const double z = (double)(m / ((long long)G.nx * G.ny));
+  const double exx = J.E[0][0], eyy = J.E[1][1], ezz = J.E[2][2];
+  const double exy = J.E[0][1], exz = J.E[0][2], eyz = J.E[1][2];
+  u[m] = x * exx + y * exy + z * exz;
+  u[m + G.ns] = x * exy + y * eyy + z * eyz;
+  u[m + 2 * G.ns] = x * exz + y * eyz + z * ezz;
+}
+
+// invert3x3 (src/elas3dxtal_pcg.f90:2046-2147); a is row-major a[i][j].
+__device__ __forceinline__ void invert3x3(const double a[3][3], double ai[3][3]) {
+  const double c11 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  const double c21 = -a[1][0] * a[2][2] + a[1][2] * a[2][0];
+  const double c31 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  const double det = a[0][0] * c11 + a[0][1] * c21 + a[0][2] * c31;
+  if (fabs(det) < 1e-14) {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) ai[i][j] = 0.0;
+    return;
+  }
+  const double inv_det = 1.0 / det;
+  const double c12 = -a[0][1] * a[2][2] + a[0][2] * a[2][1];
+  const double c22 = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+  const double c32 = -a[0][0] * a[2][1] + a[0][1] * a[2][0];
+  const double c13 = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  const double c23 = -a[0][0] * a[1][2] + a[0][2] * a[1][0];
+  const double c33 = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  ai[0][0] = c11 * inv_det;
+  ai[1][0] = c21 * inv_det;
+  ai[2][0] = c31 * inv_det;
+  ai[0][1] = c12 * inv_det;
+  ai[1][1] = c22 * inv_det;
+  ai[2][1] = c32 * inv_det;
+  ai[0][2] = c13 * inv_det;
+  ai[1][2] = c23 * inv_det;
+  ai[2][2] = c33 * inv_det;
+}
+
+// Block-Jacobi (src/elas3dxtal_pcg.f90:1498-1520): sum of the node's diagonal
+// 3x3 blocks over its 8 elements (reference order), inverted.  Stores the
+// symmetric inverse as 6 SoA planes (00 11 22 01 02 12) in FP64 and FP32.
+__global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pix, const double* __restrict__ dkd,
+                               double* __restrict__ minv, float* __restrict__ minv32) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= G.ns) return;
+  const int x = (int)(m % G.nx);
+  const int y = (int)((m / G.nx) % G.ny);
+  const int z = (int)(m / ((long long)G.nx * G.ny));
+  double M[3][3];
+  for (int ra = 0; ra < 8; ++ra) {
+    const int a = kRefToCorner[ra];
+    const int ex = wrapi(x - (a & 1), G.nx), ey = wrapi(y - ((a >> 1) & 1), G.ny),
+              ez = wrapi(z - ((a >> 2) & 1), G.nz);
+    const int ph = pix[(long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez];
+    const double* D = dkd + (long long)ph * 72 + ra * 9;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) M[i][j] = (ra == 0) ? D[i * 3 + j] : M[i][j] + D[i * 3 + j];
+  }
+  double Mi[3][3];
+  invert3x3(M, Mi);
+  const double s[6] = {Mi[0][0], Mi[1][1], Mi[2][2], Mi[0][1], Mi[0][2], Mi[1][2]};
+  for (int q = 0; q < 6; ++q) {
+    minv[m + q * G.ns] = s[q];
+    if (minv32) minv32[m + q * G.ns] = (float)s[q];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void precond3(const T* __restrict__ mi, long long m, long long ns, const T (&g)[3],
+                                         T (&z)[3]) {
+  const T a00 = mi[m], a11 = mi[m + ns], a22 = mi[m + 2 * ns];
+  const T a01 = mi[m + 3 * ns], a02 = mi[m + 4 * ns], a12 = mi[m + 5 * ns];
+  // z(i) = Minv(i,1) g1 + Minv(i,2) g2 + Minv(i,3) g3 (src/elas3dxtal_pcg.f90:1930-1932)
+  z[0] = a00 * g[0] + a01 * g[1] + a02 * g[2];
+  z[1] = a01 * g[0] + a11 * g[1] + a12 * g[2];
+  z[2] = a02 * g[0] + a12 * g[1] + a22 * g[2];
+}
+
+// ---------------------------------------------------------------------------
+// Stress (stress_OpenMP :2149-2408, stress_fullfield_OpenMP :2723-2833).
+__device__ __forceinline__ void voxel_strain(const GridDims& G, const JumpParams& J, const double* __restrict__ u,
+                                             int x, int y, int z, double (&eps)[6]) {
+  double v[3][8];
+  for (int a = 0; a < 8; ++a) {
+    const int ox = a & 1, oy = (a >> 1) & 1, oz = (a >> 2) & 1;
+    const int xx = x + ox >= G.nx ? 0 : x + ox, yy = y + oy >= G.ny ? 0 : y + oy,
+              zz = z + oz >= G.nz ? 0 : z + oz;
+    const long long mm = (long long)xx + (long long)G.nx * yy + (long long)G.nx * G.ny * zz;
+    for (int c = 0; c < 3; ++c) v[c][a] = u[mm + c * G.ns];
+  }
+  // periodic jump, x then y then z as at :2282-2323
+  if (x == G.nx - 1)
+    for (int a = 0; a < 8; ++a)
+      if (a & 1)
+        for (int c = 0; c < 3; ++c) v[c][a] += J.E[c][0] * (double)G.nx;
+  if (y == G.ny - 1)
+    for (int a = 0; a < 8; ++a)
+      if (a & 2)
+        for (int c = 0; c < 3; ++c) v[c][a] += J.E[c][1] * (double)G.ny;
+  if (z == G.nz - 1)
+    for (int a = 0; a < 8; ++a)
+      if (a & 4)
+        for (int c = 0; c < 3; ++c) v[c][a] += J.E[c][2] * (double)G.nz;
+  // centre strain = (1/4) x first-order Hadamard differences (engineering shear)
+  double dX[3], dY[3], dZ[3];
+  for (int c = 0; c < 3; ++c) {
+    double sx = 0, sy = 0, sz = 0;
+    for (int a = 0; a < 8; ++a) {
+      sx += (a & 1) ? v[c][a] : -v[c][a];
+      sy += (a & 2) ? v[c][a] : -v[c][a];
+      sz += (a & 4) ? v[c][a] : -v[c][a];
+    }
+    dX[c] = 0.25 * sx;
+    dY[c] = 0.25 * sy;
+    dZ[c] = 0.25 * sz;
+  }
+  eps[0] = dX[0];
+  eps[1] = dY[1];
+  eps[2] = dZ[2];
+  eps[3] = dZ[0] + dX[2];
+  eps[4] = dZ[1] + dY[2];
+  eps[5] = dY[0] + dX[1];
+}
+
+__global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+                                                         const double* __restrict__ cmod, int nphase,
+                                                         const double* __restrict__ u, double* partial) {
+  __shared__ double red[8];
+  double acc[12];
+  for (int t = 0; t < 12; ++t) acc[t] = 0.0;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
+       m += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(m % G.nx);
+    const int y = (int)((m / G.nx) % G.ny);
+    const int z = (int)(m / ((long long)G.nx * G.ny));
+    double eps[6];
+    voxel_strain(G, J, u, x, y, z, eps);
+    const int ph = pix[m];
+    for (int r = 0; r < 6; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < 6; ++c) s += cmod[ph + (long long)nphase * (r + 6 * c)] * eps[c];
+      acc[r] += s;
+      acc[6 + r] += eps[r];
+    }
+  }
+  for (int t = 0; t < 12; ++t) {
+    const double s = block_sum<256>(acc[t], red);
+    if (threadIdx.x == 0) partial[12 * (long long)blockIdx.x + t] = s;
+  }
+}
+
+__global__ void stress_field_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+                                    const double* __restrict__ cmod, int nphase, const double* __restrict__ u,
+                                    double* __restrict__ sigma, double* __restrict__ vm) {
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= G.ns) return;
+  const int x = (int)(m % G.nx);
+  const int y = (int)((m / G.nx) % G.ny);
+  const int z = (int)(m / ((long long)G.nx * G.ny));
+  double eps[6];
+  voxel_strain(G, J, u, x, y, z, eps);
+  const int ph = pix[m];
+  double s6[6];
+  for (int r = 0; r < 6; ++r) {
+    double s = 0.0;
+    for (int c = 0; c < 6; ++c) s += cmod[ph + (long long)nphase * (r + 6 * c)] * eps[c];
+    s6[r] = s;
+    if (sigma) sigma[m + r * G.ns] = s;
+  }
+  if (vm) {
+    const double a = s6[0] - s6[1], bq = s6[1] - s6[2], c = s6[2] - s6[0];
+    vm[m] = sqrt(0.5 * (a * a + bq * bq + c * c + 6.0 * (s6[3] * s6[3] + s6[4] * s6[4] + s6[5] * s6[5])));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent PCG (dembx_OpenMP main loop, src/elas3dxtal_pcg.f90:1574-2012).
+// One cooperative launch runs up to it_limit iterations; every block keeps an
+// identical copy of the scalars (each reduces the same partials in the same
+// order), so only two grid barriers per iteration are needed:
+//   A: h_new = z + gamma*h_old (or z), Ah = K h_new, partial h.Ah   | barrier
+//      lambda = gg/hAh (guards :1899-1907)
+//   B: u -= lambda h ; g -= lambda Ah ; z = Minv g ; partial z.g     | barrier
+//      rel_res, divergence reset (:1961-1981), gamma (:1988), stop test (:2007)
+struct PcgState {
+  double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, pad;
+  int it, status, reset, resets, cur, max_iter, divergence_reset, pad2;
+};
+
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+};
+
+// Grid-wide barrier for a cooperative launch.  Waits are bounded by a
+// wall-clock limit (globaltimer) and an iteration cap; on expiry, or when
+// another block has flagged an error, it returns false and the caller exits.
+__device__ bool grid_barrier(GridBarrier* gb, int* err, unsigned long long timeout_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned int* vgen = &gb->gen;
+    const unsigned int g0 = *vgen;
+    __threadfence();
+    const unsigned int prev = atomicAdd(&gb->count, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      const unsigned long long t0 = global_timer_ns();
+      unsigned long long spins = 0;
+      while (*vgen == g0) {
+        if (*(volatile int*)err != DEV_OK) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(128);
+        if (((++spins) & 255ull) == 0ull) {
+          if (global_timer_ns() - t0 > timeout_ns || spins > (1ull << 34)) {
+            atomicExch(err, DEV_TIMEOUT);
+            ok = 0;
+            break;
+          }
+        }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Sum of n per-block partials in a fixed order, returned to every thread.
+__device__ double reduce_broadcast(const double* partial, int n, double* red) {
+  __shared__ double s_val;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + i);
+  const double t = block_sum<NT>(s, red);
+  if (threadIdx.x == 0) s_val = t;
+  __syncthreads();
+  return s_val;
+}
+
+struct PcgArgs {
+  ApplyArgs<double> A;  // x / hnew / zv / gamma / reset set per iteration
+  double* h0;
+  double* h1;
+  double* u;
+  double* g;
+  double* z;
+  double* Ah;
+  const double* minv;
+  double* partA;  // [gridDim.x]
+  double* partB;  // [gridDim.x]
+  PcgState* st;
+  double* history;
+  GridBarrier* bar;
+  int* err;
+  int it_limit;
+  unsigned long long timeout_ns;
+};
+
+__global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
+  __shared__ ApplySmem<double> sm;
+  __shared__ double red[NT / 32];
+  __shared__ PcgState S0;
+  if (threadIdx.x == 0) S0 = *P.st;
+  __syncthreads();
+  PcgState s = S0;
+  if (s.status != PCG_RUNNING) return;
+  const GridDims& G = P.A.g;
+  const long long ns = G.ns;
+  const int it_end = min(s.it + P.it_limit, s.max_iter);
+  while (s.it < it_end) {
+    // ---- phase A: fused direction update + stencil + h.Ah
+    ApplyArgs<double> A = P.A;
+    A.x = s.cur ? P.h1 : P.h0;
+    A.hnew = s.cur ? P.h0 : P.h1;
+    A.zv = P.z;
+    A.y = P.Ah;
+    A.gamma = s.gamma;
+    A.reset = s.reset;
+    double hAh_t = 0.0;
+    for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
+      apply_tile<double, true>(A, t, sm, hAh_t);
+      __syncthreads();
+    }
+    {
+      const double bs = block_sum<NT>(hAh_t, red);
+      if (threadIdx.x == 0) P.partA[blockIdx.x] = bs;
+    }
+    if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
+      s.status = PCG_TIMEOUT;
+      break;
+    }
+    const double hAh = reduce_broadcast(P.partA, gridDim.x, red);
+    s.it += 1;
+    s.cur ^= 1;
+    s.hAh = hAh;
+    if (!isfinite(hAh)) {
+      s.status = PCG_BREAKDOWN;
+      break;
+    }
+    if (fabs(hAh) < 1e-14) {  // src/elas3dxtal_pcg.f90:1899-1902
+      s.status = PCG_HAH;
+      break;
+    }
+    const double lambda = s.gg / hAh;
+    // ---- phase B: u, g update, preconditioner, z.g
+    const double* hc = s.cur ? P.h1 : P.h0;
+    double zg_t = 0.0;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < ns;
+         m += (long long)gridDim.x * blockDim.x) {
+      const int x = (int)(m % G.nx);
+      const int y = (int)((m / G.nx) % G.ny);
+      const int zc = (int)(m / ((long long)G.nx * G.ny));
+      double ah[3] = {__ldcg(P.Ah + m), __ldcg(P.Ah + m + ns), __ldcg(P.Ah + m + 2 * ns)};
+      halo_add<double>(G, P.A.hx, P.A.hy, P.A.hd, x, y, zc, ah);
+      double gv[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long i = m + c * ns;
+        P.u[i] = P.u[i] - lambda * __ldcg(hc + i);
+        gv[c] = P.g[i] - lambda * ah[c];
+        P.g[i] = gv[c];
+      }
+      double zv[3];
+      precond3<double>(P.minv, m, ns, gv, zv);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        P.z[m + c * ns] = zv[c];
+        zg_t += zv[c] * gv[c];
+      }
+    }
+    {
+      const double bs = block_sum<NT>(zg_t, red);
+      if (threadIdx.x == 0) P.partB[blockIdx.x] = bs;
+    }
+    if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
+      s.status = PCG_TIMEOUT;
+      break;
+    }
+    const double gglast = s.gg;
+    s.gg = reduce_broadcast(P.partB, gridDim.x, red);
+    if (!isfinite(s.gg)) {
+      s.status = PCG_BREAKDOWN;
+      break;
+    }
+    const double rel_res = sqrt(s.gg / s.gg0);
+    s.rel_res = rel_res;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && P.history) P.history[s.it - 1] = rel_res;
+    if (s.divergence_reset && rel_res > 10.0 * s.rel_res_prev && s.it > 1) {
+      s.reset = 1;
+      s.resets += 1;
+    } else {
+      s.gamma = s.gg / gglast;
+      s.reset = 0;
+    }
+    s.rel_res_prev = rel_res;
+    if (rel_res < s.tol) {
+      s.status = PCG_CONVERGED;
+      break;
+    }
+  }
+  if (s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.st = s;
+}
+
+// PCG set-up (src/elas3dxtal_pcg.f90:1527-1567): z = Minv g, partial z.g.
+__global__ void __launch_bounds__(256) pcg_init_kernel(GridDims G, const double* __restrict__ minv,
+                                                       const double* __restrict__ g, double* __restrict__ z,
+                                                       double* partial) {
+  __shared__ double red[8];
+  double acc = 0.0;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
+       m += (long long)gridDim.x * blockDim.x) {
+    const double gv[3] = {g[m], g[m + G.ns], g[m + 2 * G.ns]};
+    double zv[3];
+    precond3<double>(minv, m, G.ns, gv, zv);
+    for (int c = 0; c < 3; ++c) {
+      z[m + c * G.ns] = zv[c];
+      acc += zv[c] * gv[c];
+    }
+  }
+  const double s = block_sum<256>(acc, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int n, double gg0_ref,
+                                        int criterion, float tol, int max_iter, int divergence_reset,
+                                        PcgState* st) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  const double gg = block_sum<256>(s, red);
+  if (threadIdx.x == 0) {
+    PcgState S;
+    S.gg = gg;
+    S.gg0 = (criterion == 1) ? gg : gg0_ref;
+    S.rel_res_prev = sqrt(gg / S.gg0);
+    S.rel_res = S.rel_res_prev;
+    S.gamma = 0.0;
+    S.tol = (double)tol;
+    S.hAh = 0.0;
+    S.pad = 0.0;
+    S.it = 0;
+    S.status = PCG_RUNNING;
+    S.reset = 1;  // h = z on the first step (:1554-1562)
+    S.resets = 0;
+    S.cur = 0;
+    S.max_iter = max_iter;
+    S.divergence_reset = divergence_reset;
+    S.pad2 = 0;
+    *st = S;
+  }
+}
+
+}  // namespace e3d

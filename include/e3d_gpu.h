@@ -1,0 +1,187 @@
+/*
+ * e3d_gpu.h -- C ABI of the GB300 (sm_103a) voxel-FE elasticity solver.
+ *
+ * Drop-in boundary for the hot path of ELAS3D-Xtal (src/elas3dxtal_pcg.f90).
+ * The reference exposes no library: its "API" is five Fortran subroutines
+ * called by `program elas3d` on a shared derived type `e3d`.  Each entry
+ * point below replaces one of them and keeps its meaning; the reference
+ * subroutine is cited beside it.  Plain C types only (int32_t, int64_t,
+ * double*, opaque handle), so Fortran binds it through iso_c_binding, Python
+ * through ctypes and C++ directly.
+ *
+ * Conventions (same as the reference's arrays, src/elas3dxtal_pcg.f90:155-181):
+ *  - grid of nx*ny*nz nodes, fully periodic, node/voxel (i,j,k) (0-based) has
+ *    linear index m = i + nx*(j + ny*k)  (Fortran column order);
+ *  - vectors of 3 dof per node are component-major ("SoA"), i.e. Fortran
+ *    u(ns,3): x[c*ns + m];
+ *  - phase ids in pix are 1-based, in [1, nphase]; phase nphase is the
+ *    inclusion / pore phase (E1, nu1 -- zero stiffness by default);
+ *  - orientations are Rodrigues vectors r = q_xyz/q_w, 3 per grain, grains
+ *    1..nphase-1 (src/elas3dxtal_pcg.f90:2538);
+ *  - strains are TENSOR components (exx, eyy, ezz, exz, eyz, exy), as
+ *    e3d%exx.. in the reference; averaged outputs use engineering shear and
+ *    Voigt order xx, yy, zz, xz, yz, xy (src/elas3dxtal_pcg.f90:2235-2237).
+ *
+ * Ownership: host arrays are caller-owned and copied in/out; device state is
+ * owned by the handle.  Threading: one handle per host thread; all work runs
+ * on the handle's CUDA stream and every call returns after it completes.
+ * Errors: every call returns an E3D_* status (the reference `stop`s instead).
+ */
+#ifndef E3D_GPU_H
+#define E3D_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define E3D_OK 0
+#define E3D_ERR_INPUT 1     /* bad argument / size / phase id out of range   */
+#define E3D_ERR_OOM 2       /* device allocation failed or over hbm_budget    */
+#define E3D_ERR_BREAKDOWN 3 /* NaN/Inf in h.Ah or z.g                         */
+#define E3D_ERR_MAXITER 4   /* solve stopped at max_iter without converging   */
+#define E3D_ERR_TIMEOUT 5   /* a device-side wait exceeded its limit          */
+#define E3D_ERR_CUDA 6      /* CUDA runtime error (see e3d_last_cuda_error)   */
+#define E3D_ERR_STATE 7     /* call out of order (e.g. solve before energy)   */
+
+/* ---- solve exit reasons (e3d_solve_stats_t.exit_reason) ---- */
+#define E3D_EXIT_CONVERGED 0 /* rel_res < tol (src/elas3dxtal_pcg.f90:2007)     */
+#define E3D_EXIT_HAH_GUARD 1 /* |h.Ah| < 1e-14 (src/elas3dxtal_pcg.f90:1899)    */
+#define E3D_EXIT_MAXITER 2   /* ldemb iterations (src/elas3dxtal_pcg.f90:1574)  */
+#define E3D_EXIT_BREAKDOWN 3 /* non-finite scalar                               */
+#define E3D_EXIT_TIMEOUT 4   /* device wait limit                               */
+#define E3D_EXIT_RUNNING 5   /* iteration budget of an e3d_iterate call used up */
+
+/* ---- stopping criterion ---- */
+#define E3D_CRIT_REF 0         /* sqrt(z.g / |g0|^2), the reference's test (:1949, :452) */
+#define E3D_CRIT_PRECOND_REL 1 /* sqrt(z.g / z0.g0), true preconditioned relative     */
+
+/* ---- arithmetic ---- */
+#define E3D_PREC_FP64 0  /* FP64 everywhere (the reference's arithmetic)           */
+#define E3D_PREC_MIXED 1 /* FP32 stencil + preconditioner inside FP64 refinement   */
+
+typedef struct e3d_problem {
+  int32_t nx, ny, nz;       /* nodes per direction, ns = nx*ny*nz (md in the ref)  */
+  int32_t nphase;           /* grains + 1                                           */
+  int32_t flag_m;           /* 0 isotropic matrix, 1 rotated cubic polycrystal     */
+  int32_t criterion;        /* E3D_CRIT_*                                          */
+  int32_t precision;        /* E3D_PREC_*                                          */
+  int32_t divergence_reset; /* 1: h = z when rel_res grows > 10x (:1961-1981)      */
+  int32_t max_iter;         /* ldemb (:141)                                        */
+  int32_t device;           /* CUDA device ordinal                                 */
+  float tol;                /* single precision, as `real :: tol` (:148)           */
+  int32_t refine_every;     /* MIXED: FP64 residual replacement period (0 = 50)    */
+  double c11, c12, c44;     /* cubic constants, Pa (:100-102)                      */
+  double e1, nu1;           /* inclusion Young's modulus / Poisson ratio (:114-115)*/
+  double strain[6];         /* exx, eyy, ezz, exz, eyz, exy (tensor) (:394-399)    */
+  int64_t hbm_budget;       /* bytes the handle may allocate; 0 = unlimited        */
+} e3d_problem_t;
+
+typedef struct e3d_solve_stats {
+  int32_t iterations;  /* Lstep (:1575)                                          */
+  int32_t exit_reason; /* E3D_EXIT_*                                             */
+  int32_t resets;      /* divergence resets (:1978)                              */
+  int32_t refinements; /* MIXED: FP64 residual replacements performed            */
+  double gg;           /* final z.g (gg returned by dembx_OpenMP)                */
+  double gg0;          /* denominator of the criterion                           */
+  double rel_res;      /* sqrt(gg/gg0), the criterion value at exit              */
+  double true_rel;     /* |g| / |g0| from the recurrence residual                */
+  double ms_setup;     /* block-Jacobi build + initial z, milliseconds           */
+  double ms_iter;      /* PCG iterations, milliseconds                           */
+} e3d_solve_stats_t;
+
+typedef struct e3d_handle e3d_handle_t;
+
+/* Fills p with the reference's defaults (src/elas3dxtal_pcg.f90:77-148):
+ * C11/C12/C44 = 206/133/119 GPa, E1 = nu1 = 0, ezz = 1e-3, tol = 1e-8 (float),
+ * ldemb = 10000, flag_m = 1, REF criterion, FP64, divergence reset on. */
+void e3d_problem_defaults(e3d_problem_t* p, int32_t nx, int32_t ny, int32_t nz,
+                          int32_t nphase);
+
+/* Allocates the device state of one problem (the allocate() block of
+ * `program elas3d`, src/elas3dxtal_pcg.f90:242-256).  The neighbour table ib
+ * (:326-369) is not stored: kernels compute periodic neighbours. */
+int32_t e3d_create(e3d_handle_t** h, const e3d_problem_t* p);
+int32_t e3d_destroy(e3d_handle_t* h);
+
+/* Phase map + orientations, as read by ppixel_hdf5 (:2879-2990): pix has ns
+ * entries in [1, nphase] (checked as at :2986-2989), rodrigues has
+ * 3*(nphase-1) entries (ignored when flag_m == 0, may be NULL then). */
+int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rodrigues);
+
+/* femat_OpenMP (:555-1104): cmod (rotatestiffnessby, :2470-2637), element
+ * stiffness dk, periodic-jump force b and constant C, all on the device. */
+int32_t e3d_femat(e3d_handle_t* h);
+
+/* Affine initial guess u = E.x (driver, :423-438). */
+int32_t e3d_init_affine(e3d_handle_t* h);
+
+/* energy_OpenMP (:1107-1353): gb = K u + b and utot = C + sum(u.Ku/2 + b.u).
+ * Also returns gg = sum(gb^2), which the driver stores as gg0 (:452-453);
+ * the handle keeps it as the REF criterion denominator for e3d_solve. */
+int32_t e3d_energy(e3d_handle_t* h, double* utot, double* gg);
+
+/* dembx_OpenMP with kkk = 1 (:1356-2043): block-Jacobi build (:1498-1520,
+ * invert3x3 :2046-2147), then PCG on u and gb until the criterion, the hAh
+ * guard or max_iter.  Returns E3D_OK (converged or hAh guard),
+ * E3D_ERR_MAXITER, E3D_ERR_BREAKDOWN or E3D_ERR_TIMEOUT; st may be NULL. */
+int32_t e3d_solve(e3d_handle_t* h, e3d_solve_stats_t* st);
+
+/* Split form of e3d_solve for callers that interleave work or time single
+ * iterations: e3d_solve_begin does the setup, e3d_iterate runs at most n
+ * iterations (exit_reason E3D_EXIT_RUNNING when the budget ran out). */
+int32_t e3d_solve_begin(e3d_handle_t* h);
+int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st);
+
+/* stress_OpenMP (:2149-2408): volume-averaged stress (Pa) and engineering
+ * strain, Voigt xx, yy, zz, xz, yz, xy. */
+int32_t e3d_stress(e3d_handle_t* h, double strav[6], double epsav[6]);
+
+/* stress_fullfield_OpenMP compute part (:2723-2833): sigma(ns,6) (SoA) and
+ * von Mises vm(ns).  Either pointer may be NULL.  The HDF5 write is left to
+ * the caller. */
+int32_t e3d_stress_field(e3d_handle_t* h, double* sigma, double* vm);
+
+/* The whole driver flow of `program elas3d` without file I/O (:417-514):
+ * femat, affine guess, energy, gg0, dembx, energy, stress.  out6[0..5] =
+ * strav, out6[6..11] = epsav; utot[0] initial energy, utot[1] final energy. */
+int32_t e3d_run(e3d_handle_t* h, double utot[2], double out12[12], e3d_solve_stats_t* st);
+
+/* Matrix-free y = K x (the stencil of :1585-1883 without b), host buffers of
+ * 3*ns doubles.  e3d_apply_device takes device pointers instead. */
+int32_t e3d_apply(e3d_handle_t* h, const double* x, double* y);
+int32_t e3d_apply_device(e3d_handle_t* h, const double* d_x, double* d_y);
+
+/* State transfer (3*ns doubles each unless noted). */
+int32_t e3d_set_u(e3d_handle_t* h, const double* u);
+int32_t e3d_get_u(e3d_handle_t* h, double* u);
+int32_t e3d_get_g(e3d_handle_t* h, double* g);
+int32_t e3d_get_b(e3d_handle_t* h, double* b);
+int32_t e3d_get_C(e3d_handle_t* h, double* C);
+/* cmod(nphase,6,6) and dk(nphase,8,3,8,3) in the reference's Fortran layout. */
+int32_t e3d_get_cmod(e3d_handle_t* h, double* cmod);
+int32_t e3d_get_dk(e3d_handle_t* h, double* dk);
+/* Block-Jacobi inverses in the reference's M_block_inv(ns,3,3) layout (9*ns). */
+int32_t e3d_get_minv(e3d_handle_t* h, double* minv);
+/* Per-iteration rel_res history of the last solve (cgitr file, :2019-2021);
+ * copies min(n, iterations) values, returns the count through *count. */
+int32_t e3d_get_history(e3d_handle_t* h, double* hist, int32_t n, int32_t* count);
+
+/* Device pointers of the state vectors (3*ns doubles each, SoA), for callers
+ * that keep inputs resident in HBM. */
+int32_t e3d_device_ptrs(e3d_handle_t* h, double** d_u, double** d_g, double** d_b);
+
+/* Bytes of device memory the handle holds. */
+int64_t e3d_device_bytes(const e3d_handle_t* h);
+
+/* Number of kernel launches issued by the handle so far. */
+int64_t e3d_launch_count(const e3d_handle_t* h);
+
+const char* e3d_strerror(int32_t status);
+/* Text of the last CUDA error seen by any handle in this thread. */
+const char* e3d_last_cuda_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,59 @@
+/*
+ * e3d_micro.h -- seeded synthetic microstructures for the voxel-FE solver.
+ *
+ * The reference builds its inputs with MATLAB + MTEX (src/microstructure_gen.m)
+ * and stores them as HDF5 /pix (int32, 1-based phase per voxel) and
+ * /orientation (float64, one Rodrigues vector per grain)
+ * (src/microstructure_gen.m:866-892).  These host routines write the same two
+ * arrays, deterministically from a 64-bit seed, so that every workload can be
+ * regenerated on any machine instead of being shipped as a file.
+ *
+ * Grid convention: nodes == voxels (fully periodic), voxel (i,j,k) has centre
+ * (i+0.5, j+0.5, k+0.5) in a box of side (nx, ny, nz) voxels, linear index
+ * m = i + nx*(j + ny*k).  Grains are phases 1..ngrains; the pore phase is
+ * ngrains+1 (zero stiffness in the solver).
+ */
+#ifndef E3D_MICRO_H
+#define E3D_MICRO_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Periodic Voronoi (laguerre_sigma == 0) or Laguerre/power-Voronoi
+ * (laguerre_sigma > 0: grain volumes ~ lognormal(sigma)) tessellation.
+ * Seeds are uniform in the box; each voxel centre takes the grain of the
+ * nearest seed under the minimum-image distance (power distance for Laguerre);
+ * ties go to the lower grain id.  Orientations are uniform on SO(3): an
+ * isotropic unit quaternion with q_w >= 0, stored as Rodrigues r = q_xyz/q_w
+ * (the reference's convention, src/microstructure_gen.m:774-800).
+ * pix: nx*ny*nz int32; rod: 3*ngrains doubles.  Returns 0 on success. */
+int32_t e3d_micro_grains(int32_t nx, int32_t ny, int32_t nz, int32_t ngrains,
+                         double laguerre_sigma, uint64_t seed, int32_t* pix,
+                         double* rod);
+
+/* Adds periodic spherical pores (radius ~ lognormal(log_mu, log_sigma) voxels,
+ * uniform centres) until at least target_frac of the voxels carry pore_phase.
+ * Returns the number of pores placed (< 0 on error). */
+int32_t e3d_micro_spherical_pores(int32_t nx, int32_t ny, int32_t nz,
+                                  double target_frac, double log_mu,
+                                  double log_sigma, int32_t pore_phase,
+                                  uint64_t seed, int32_t* pix);
+
+/* Adds periodic ellipsoidal voids with semi-axes (aspect*a, a, a), a ~
+ * lognormal(log_mu, log_sigma) voxels, uniformly random orientation, until at
+ * least target_frac of the voxels carry pore_phase.  Returns the count. */
+int32_t e3d_micro_ellipsoidal_pores(int32_t nx, int32_t ny, int32_t nz,
+                                    double target_frac, double aspect,
+                                    double log_mu, double log_sigma,
+                                    int32_t pore_phase, uint64_t seed,
+                                    int32_t* pix);
+
+/* Bunge Euler angles (phi1, Phi, phi2; radians) -> Rodrigues vectors, for
+ * callers whose orientation files hold Euler angles.  n orientations. */
+void e3d_euler_to_rodrigues(int32_t n, const double* euler, double* rod);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,207 @@
+"""Parity of the CUDA library (called through the C ABI) against the CPU
+oracle on the same seeded inputs.
+
+Tolerances (spec contract for the plain FP64 path):
+  K.u                      1e-12 relative (norm-wise)
+  dk, cmod, b, C, Minv     1e-12 relative (max-norm over the array)
+  converged energy, <sigma> 1e-9 relative, iteration count within +-2
+"""
+import numpy as np
+import pytest
+
+import elas3d_xtal_gb300 as e3d
+import oracle as O
+from elas3d_xtal_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+KU_TOL = 1e-12
+TAB_TOL = 1e-12
+SOLVE_TOL = 1e-9
+
+
+def _oracle_problem(p: e3d.Problem) -> O.Problem:
+    s = p.strain
+    return O.Problem(p.nx, p.ny, p.nz, p.nphase, flag_m=p.flag_m, c11=p.c11, c12=p.c12, c44=p.c44,
+                     e1=p.e1, nu1=p.nu1, exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5],
+                     tol=p.tol, ldemb=p.max_iter, criterion=p.criterion,
+                     divergence_reset=p.divergence_reset)
+
+
+def _rel(a, b):
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def _relmax(a, b):
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    den = np.abs(b).max()
+    return np.abs(a - b).max() / (den if den > 0 else 1.0)
+
+
+def random_case(nx, ny, nz, ngrains, seed, pores=True, strain=None, **kw):
+    rng = np.random.default_rng(seed)
+    nphase = ngrains + 1
+    hi = nphase + 1 if pores else nphase
+    pix = rng.integers(1, hi, size=nx * ny * nz).astype(np.int32)
+    rod = rng.normal(size=3 * ngrains)
+    if strain is None:
+        strain = tuple(rng.normal(size=6) * 1e-3)
+    p = e3d.Problem(nx, ny, nz, nphase, strain=strain, **kw)
+    return p, pix, rod
+
+
+def _pair(p, pix, rod):
+    g = e3d.Elas3D(p).upload(pix, rod).femat()
+    o = O.Oracle(_oracle_problem(p), pix, rod).femat()
+    return g, o
+
+
+SHAPES = [
+    (4, 4, 4, 3),
+    (5, 7, 9, 4),
+    (8, 8, 8, 6),
+    (33, 17, 9, 10),   # partial tiles in x and y
+    (40, 9, 19, 5),
+    (1, 3, 4, 2),      # degenerate periodic directions
+    (2, 2, 2, 2),
+    (64, 16, 3, 12),
+]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_femat_tables(shape):
+    nx, ny, nz, ng = shape
+    p, pix, rod = random_case(nx, ny, nz, ng, seed=nx * 100 + ny)
+    g, o = _pair(p, pix, rod)
+    assert _relmax(g.get_cmod(), o.cmod_array()) < TAB_TOL
+    assert _relmax(g.get_dk(), o.dk_array()) < TAB_TOL
+    assert _rel(g.get_b(), o.b) < TAB_TOL
+    assert abs(g.get_C() - o.C) <= 1e-11 * max(abs(o.C), 1e-300)
+    g.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_apply_matches_oracle(shape):
+    nx, ny, nz, ng = shape
+    p, pix, rod = random_case(nx, ny, nz, ng, seed=7 + nx)
+    g, o = _pair(p, pix, rod)
+    x = W.random_field(p.ns, seed=11)
+    y = g.apply(x)
+    y_ref = o.apply(x)
+    assert _rel(y, y_ref) < KU_TOL
+    g.close()
+
+
+def test_apply_isotropic_flag0():
+    p, pix, rod = random_case(12, 10, 6, 1, seed=3, flag_m=0)
+    p.e1, p.nu1 = 50e9, 0.25
+    g, o = _pair(p, pix, None)
+    x = W.random_field(p.ns, seed=5)
+    assert _rel(g.apply(x), o.apply(x)) < KU_TOL
+    assert _relmax(g.get_cmod(), o.cmod_array()) < TAB_TOL
+
+
+def test_energy_and_gradient():
+    p, pix, rod = random_case(20, 12, 10, 6, seed=21)
+    g, o = _pair(p, pix, rod)
+    g.init_affine()
+    utot, gg = g.energy()
+    u0 = o.affine_u()
+    assert _rel(g.get_u(), u0) < 1e-15  # FMA contraction on the device
+    g_ref, ut_ref = o.energy(u0)
+    assert abs(utot - ut_ref) <= 1e-11 * abs(ut_ref)
+    assert _rel(g.get_g(), g_ref) < 1e-11
+    assert abs(gg - float(g_ref @ g_ref)) <= 1e-11 * float(g_ref @ g_ref)
+
+
+def test_block_jacobi_inverse():
+    p, pix, rod = random_case(9, 10, 11, 4, seed=31)
+    g, o = _pair(p, pix, rod)
+    g.init_affine()
+    g.energy()
+    g.solve_begin()
+    minv = g.get_minv()
+    ref = o.block_jacobi().reshape(3, 3, p.ns).transpose(2, 1, 0)
+    assert _relmax(minv, ref) < TAB_TOL
+    # pore-only nodes: singular block -> zero inverse (src/elas3dxtal_pcg.f90:2106-2109)
+    assert np.all(np.isfinite(minv))
+
+
+@pytest.mark.parametrize("criterion", [e3d.CRIT_REF, e3d.CRIT_PRECOND_REL])
+def test_full_solve_polycrystal(criterion):
+    p, pix, rod = W.c1(n=16, ngrains=12, seed=5)
+    p.criterion = criterion
+    p.strain = (1e-3, 0, 0, 0, 0, 0)
+    g = e3d.Elas3D(p).upload(pix, rod)
+    res = g.run()
+    ref = O.run(_oracle_problem(p), pix, rod)
+    assert res["exit_reason"] == e3d.EXIT_CONVERGED
+    assert abs(res["iterations"] - ref["lstep"]) <= 2
+    assert abs(res["utot0"] - ref["utot0"]) <= SOLVE_TOL * abs(ref["utot0"])
+    assert abs(res["utot"] - ref["utot"]) <= SOLVE_TOL * abs(ref["utot"])
+    assert _rel(res["strav"], ref["strav"]) < SOLVE_TOL
+    assert _rel(res["epsav"], ref["epsav"]) < SOLVE_TOL
+    hist = g.history()
+    assert hist.size == res["iterations"]
+    g.close()
+
+
+def test_full_solve_with_pores_and_shear():
+    p, pix, rod = W.c2(n=24, ngrains=20, seed=9)
+    p.strain = (2e-4, -1e-4, 3e-4, 1e-4, -2e-4, 5e-5)
+    g = e3d.Elas3D(p).upload(pix, rod)
+    res = g.run()
+    ref = O.run(_oracle_problem(p), pix, rod)
+    assert res["exit_reason"] == ref["exit_reason"] == 0
+    assert abs(res["iterations"] - ref["lstep"]) <= 2
+    assert abs(res["utot"] - ref["utot"]) <= SOLVE_TOL * abs(ref["utot"])
+    assert _rel(res["strav"], ref["strav"]) < SOLVE_TOL
+
+
+def test_stress_fields():
+    p, pix, rod = random_case(10, 11, 12, 5, seed=41)
+    g, o = _pair(p, pix, rod)
+    u = W.random_field(p.ns, seed=3) * 1e-3
+    g.set_u(u)
+    s, e = g.stress()
+    s_ref, e_ref = o.stress(u)
+    assert _rel(s, s_ref) < 1e-12
+    assert _rel(e, e_ref) < 1e-12
+    sig, vm = g.stress_fullfield()
+    sig_ref, vm_ref = o.stress_fullfield(u)
+    assert _rel(sig, sig_ref) < 1e-12
+    assert _rel(vm, vm_ref) < 1e-12
+
+
+def test_hah_guard_homogeneous():
+    # one phase, affine u is the exact solution: g0 = 0, z = 0, h.Ah = 0 ->
+    # the reference exits at its hAh guard after one step (src/elas3dxtal_pcg.f90:1899)
+    p = e3d.Problem(8, 8, 8, 2, strain=(1e-3, 0, 0, 0, 0, 0))
+    pix = np.ones(p.ns, np.int32)
+    rod = np.array([0.1, 0.2, 0.3])
+    g = e3d.Elas3D(p).upload(pix, rod)
+    res = g.run()
+    ref = O.run(_oracle_problem(p), pix, rod)
+    assert res["exit_reason"] == e3d.EXIT_HAH_GUARD
+    assert ref["exit_reason"] == 1 and ref["lstep"] == 1
+    assert res["iterations"] == 1
+
+
+def test_iterate_in_chunks_equals_single_solve():
+    p, pix, rod = W.c1(n=16, ngrains=8, seed=2)
+    a = e3d.Elas3D(p).upload(pix, rod)
+    ra = a.run()
+    b = e3d.Elas3D(p).upload(pix, rod).femat().init_affine()
+    b.energy()
+    b.solve_begin()
+    st = None
+    for _ in range(1000):
+        st = b.iterate(3)
+        if st["exit_reason"] != e3d.EXIT_RUNNING:
+            break
+    assert st["iterations"] == ra["iterations"]
+    assert np.array_equal(a.get_u(), b.get_u())
