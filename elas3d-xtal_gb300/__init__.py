@@ -51,7 +51,7 @@ EXPORTED_SYMBOLS = (
     "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
-    "e3d_device_bytes", "e3d_launch_count", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_device_bytes", "e3d_launch_count", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
     "e3d_euler_to_rodrigues",
 )
@@ -127,6 +127,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_device_bytes.restype = C.c_int64
     L.e3d_launch_count.argtypes = [vp]
     L.e3d_launch_count.restype = C.c_int64
+    L.e3d_probe_peaks.argtypes = [C.c_int32, dp, dp]
     L.e3d_strerror.argtypes = [C.c_int32]
     L.e3d_strerror.restype = C.c_char_p
     L.e3d_last_cuda_error.argtypes = []
@@ -418,6 +419,13 @@ def micro_ellipsoidal_pores(pix, nx, ny, nz, frac, pore_phase, seed, aspect=4.0,
     if rc < 0:
         raise RuntimeError(f"e3d_micro_ellipsoidal_pores failed ({rc})")
     return rc
+
+
+def probe_peaks(device: int = 0):
+    """Measured (fp64, fp32) FMA throughput in TFLOP/s."""
+    a, b = C.c_double(), C.c_double()
+    _check(load_library().e3d_probe_peaks(device, C.byref(a), C.byref(b)), "e3d_probe_peaks")
+    return a.value, b.value
 
 
 def euler_to_rodrigues(euler: np.ndarray) -> np.ndarray:

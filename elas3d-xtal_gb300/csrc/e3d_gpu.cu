@@ -725,3 +725,59 @@ int32_t e3d_device_ptrs(e3d_handle_t* h, double** d_u, double** d_g, double** d_
 }
 
 }  // extern "C"
+
+namespace {
+
+// Peak-rate probes: independent FMA chains (8 per thread) so the pipe, not
+// latency, limits the rate.  The result is stored so nothing is elided.
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+  T v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = (T)(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = fma(v[k], a, b);
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += v[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+int32_t run_probe(int device, double* tflops) {
+  cudaDeviceProp prop{};
+  E3D_CUDA(cudaGetDeviceProperties(&prop, device));
+  const int blocks = prop.multiProcessorCount * 8, threads = 256;
+  T* out = nullptr;
+  E3D_CUDA(cudaMalloc(&out, sizeof(T) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int iters = sizeof(T) == 8 ? 4096 : 65536;
+  fma_probe_kernel<T><<<blocks, threads>>>(out, iters / 16, (T)0.999999, (T)1e-7);  // warm-up
+  cudaEventRecord(e0);
+  fma_probe_kernel<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "probe");
+  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return E3D_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops) {
+  if (!fp64_tflops || !fp32_tflops) return E3D_ERR_INPUT;
+  E3D_CUDA(cudaSetDevice(device));
+  int32_t rc = run_probe<double>(device, fp64_tflops);
+  if (rc) return rc;
+  return run_probe<float>(device, fp32_tflops);
+}

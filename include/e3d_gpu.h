@@ -177,6 +177,10 @@ int64_t e3d_device_bytes(const e3d_handle_t* h);
 /* Number of kernel launches issued by the handle so far. */
 int64_t e3d_launch_count(const e3d_handle_t* h);
 
+/* Measured FP64 and FP32 FMA throughput of the device (TFLOP/s, FMA = 2
+ * flops), the compute roofline denominators of the stencil. */
+int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops);
+
 const char* e3d_strerror(int32_t status);
 /* Text of the last CUDA error seen by any handle in this thread. */
 const char* e3d_last_cuda_error(void);
