@@ -52,6 +52,7 @@ EXPORTED_SYMBOLS = (
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
     "e3d_device_bytes", "e3d_launch_count", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_apply_noalloc",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
     "e3d_euler_to_rodrigues",
 )
@@ -128,6 +129,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_launch_count.argtypes = [vp]
     L.e3d_launch_count.restype = C.c_int64
     L.e3d_probe_peaks.argtypes = [C.c_int32, dp, dp]
+    L.e3d_apply_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp]
     L.e3d_strerror.argtypes = [C.c_int32]
     L.e3d_strerror.restype = C.c_char_p
     L.e3d_last_cuda_error.argtypes = []

@@ -48,12 +48,16 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    cu_obj = os.path.join(OUT, "e3d_gpu.o")
+    cu_units = ["e3d_gpu", "e3d_noalloc"]
+    cu_objs = [os.path.join(OUT, u + ".o") for u in cu_units]
     cpp_obj = os.path.join(OUT, "microgen.o")
-    cu_cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, "e3d_gpu.cu"), "-o", cu_obj]
-    if ptxas_info:
-        cu_cmd[1:1] = ["-Xptxas", "-v"]
+    cu_cmds = []
+    for u, o in zip(cu_units, cu_objs):
+        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+               "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, u + ".cu"), "-o", o]
+        if ptxas_info:
+            cmd[1:1] = ["-Xptxas", "-v"]
+        cu_cmds.append(cmd)
     cpp_cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I", INCLUDE,
                "-c", os.path.join(CSRC, "microgen.cpp"), "-o", cpp_obj]
 
@@ -63,9 +67,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r.stdout + r.stderr
 
-    with ThreadPoolExecutor(2) as ex:
-        logs = list(ex.map(run, [cu_cmd, cpp_cmd]))
-    link = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", cu_obj, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
+    with ThreadPoolExecutor(len(cu_cmds) + 1) as ex:
+        logs = list(ex.map(run, [*cu_cmds, cpp_cmd]))
+    link = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *cu_objs, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
     logs.append(run(link))
     os.replace(LIB + ".tmp", LIB)
     if verbose or ptxas_info:

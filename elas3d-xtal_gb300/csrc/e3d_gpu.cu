@@ -28,6 +28,12 @@ struct DevBuf {
 
 }  // namespace
 
+// Error text for e3d_last_cuda_error, also used by the other translation units.
+void e3d_record_error_text(const char* text) { g_last_cuda_error = text ? text : ""; }
+void e3d_record_cuda_error(const char* what, cudaError_t e) {
+  g_last_cuda_error = std::string(what) + ": " + cudaGetErrorString(e);
+}
+
 struct e3d_handle {
   e3d_problem_t prob{};
   GridDims G{};

@@ -177,6 +177,30 @@ int64_t e3d_device_bytes(const e3d_handle_t* h);
 /* Number of kernel launches issued by the handle so far. */
 int64_t e3d_launch_count(const e3d_handle_t* h);
 
+/* No counterpart in the reference.  y = K x, the same matrix-free stencil as
+ * e3d_apply_device, for callers that must not allocate device memory: a host
+ * framework that owns every device allocation and forbids library-side
+ * cudaMalloc (which also synchronises the device), or a serving loop that
+ * admits work under a fixed HBM budget.  Nothing is allocated: the caller
+ * passes device pointers to its inputs and output --
+ *   d_pix  ns int32 phase ids, 1-based, in [1, nphase] (checked),
+ *   d_cmod 36*nphase doubles, cmod(nphase,6,6) in the reference layout
+ *          (e3d_get_cmod returns it),
+ *   d_x, d_y 3*ns doubles (SoA),
+ * and the scaled stiffness table and tile halos live in one static device
+ * array of E3D_NOALLOC_SCRATCH_BYTES per GPU, held from library load to
+ * process exit.  A grid whose scratch (about 41*3*ns/256 doubles of halos plus
+ * 108*(nphase+1) doubles of table -- e.g. 128^3 with up to 4096 phases) does
+ * not fit is rejected with E3D_ERR_INPUT and e3d_last_cuda_error() says why.
+ * Runs on `stream` (a cudaStream_t, NULL = legacy default) of the current
+ * device and returns after it completes.  The first call on each device looks
+ * up the array's device address (make it before any stream capture).  Calls
+ * share the array: calls that overlap on the GPU race. */
+#define E3D_NOALLOC_SCRATCH_BYTES (16LL * 1024 * 1024)
+int32_t e3d_apply_noalloc(int32_t nx, int32_t ny, int32_t nz, int32_t nphase,
+                          const int32_t* d_pix, const double* d_cmod,
+                          const double* d_x, double* d_y, void* stream);
+
 /* Measured FP64 and FP32 FMA throughput of the device (TFLOP/s, FMA = 2
  * flops), the compute roofline denominators of the stencil. */
 int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops);
