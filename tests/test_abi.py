@@ -1,0 +1,66 @@
+"""The C-ABI library loads on a machine without a GPU and exports every
+function declared in include/*.h (no compute calls)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+import elas3d_xtal_gb300 as e3d
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in ("e3d_gpu.h", "e3d_micro.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(e3d_[A-Za-z0-9_]+)\s*\(", text))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(e3d.LIB_PATH):
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("e3d_build", os.path.join(ROOT, "elas3d-xtal_gb300", "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        try:
+            mod.build()
+        except RuntimeError as ex:
+            pytest.skip(f"cannot build the library here: {ex}")
+    return e3d.load_library()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    declared = _declared()
+    assert len(declared) >= 30
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    assert declared == set(e3d.EXPORTED_SYMBOLS)
+
+
+def test_exports_match_nm(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", e3d.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln and ln.split()[-1].startswith("e3d_")}
+    assert _declared() <= exported
+
+
+def test_strerror_and_defaults_without_gpu(lib):
+    assert e3d.strerror(e3d.E3D_ERR_OOM).startswith("device memory")
+    p = e3d.ProblemC()
+    lib.e3d_problem_defaults(p, 10, 11, 12, 5)
+    assert (p.nx, p.ny, p.nz, p.nphase) == (10, 11, 12, 5)
+    assert abs(p.tol - 1e-8) < 1e-15 and p.max_iter == 10000 and p.strain[2] == 1e-3
+    assert p.c11 == 206e9 and p.flag_m == 1
+
+
+def test_struct_layout_matches_header(lib):
+    import ctypes as C
+
+    # e3d_problem_t: 12 int32/float (48 B) + 11 doubles (88 B) + int64 = 144 B
+    assert C.sizeof(e3d.ProblemC) == 144
+    assert C.sizeof(e3d.SolveStatsC) == 16 + 6 * 8

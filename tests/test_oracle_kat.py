@@ -1,0 +1,184 @@
+"""The CPU oracle against analytical known-answer tests and the independent
+scipy restatement (oracle/np_ref.py).  The reference ships no golden vectors,
+so these pin the oracle (CPU only)."""
+import numpy as np
+import pytest
+
+import np_ref as R
+import oracle as O
+
+C11, C12, C44 = 206e9, 133e9, 119e9
+
+
+def _rand_problem(nx, ny, nz, ng, seed, pores=True, strain=None, **kw):
+    rng = np.random.default_rng(seed)
+    nphase = ng + 1
+    pix = rng.integers(1, nphase + (1 if pores else 0), size=nx * ny * nz).astype(np.int32)
+    rod = rng.normal(size=3 * ng)
+    s = rng.normal(size=6) * 1e-3 if strain is None else np.asarray(strain, float)
+    p = O.Problem(nx, ny, nz, nphase, exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5], **kw)
+    return p, pix, rod, s
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+# ---------------------------------------------------------------- stiffness
+def test_rotation_matches_tensor_rotation_with_xz_yz_swap():
+    """rotatestiffnessby equals P R(Q^T)[C] P (xz/yz slots swapped)."""
+    rng = np.random.default_rng(0)
+    rod = rng.normal(size=3 * 5)
+    got = O.rotate_stiffness(rod, C11, C12, C44)
+    Cc = R.cubic_voigt(C11, C12, C44)
+    for g in range(5):
+        ref = R.reference_rotated(Cc, rod[3 * g:3 * g + 3])
+        assert np.abs(got[g] - ref).max() < 1e-12 * C11
+
+
+def test_zener_one_is_orientation_independent():
+    c44 = (C11 - C12) / 2.0
+    rng = np.random.default_rng(1)
+    got = O.rotate_stiffness(rng.normal(size=12), C11, C12, c44)
+    iso = R.cubic_voigt(C11, C12, c44)
+    assert np.abs(got - iso).max() < 1e-12 * C11
+
+
+def test_dk_matches_gauss_and_is_psd_with_six_rigid_modes():
+    p, pix, rod, _ = _rand_problem(3, 3, 3, 4, seed=2)
+    o = O.Oracle(p, pix, rod).femat()
+    dk = o.dk_array()
+    cm = o.cmod_array()
+    for ph in range(p.nphase - 1):
+        K = dk[ph].reshape(24, 24)
+        Kg = R.element_stiffness(cm[ph])
+        assert np.abs(K - Kg).max() < 1e-13 * np.abs(Kg).max()
+        w = np.linalg.eigvalsh(0.5 * (K + K.T))
+        assert (w > -1e-6 * w.max()).all()
+        assert (np.abs(w) < 1e-9 * w.max()).sum() == 6
+    assert np.abs(dk[p.nphase - 1]).max() == 0.0  # zero-stiffness pore phase
+
+
+def test_cmod_matches_independent_table():
+    for flag in (0, 1):
+        p, pix, rod, _ = _rand_problem(2, 2, 2, 3, seed=3, flag_m=flag)
+        p.e1, p.nu1 = 30e9, 0.2
+        o = O.Oracle(p, pix, rod).femat()
+        ref = R.cmod_table(p.nphase, flag, p.c11, p.c12, p.c44, rod, p.e1, p.nu1)
+        assert np.abs(o.cmod_array() - ref).max() < 1e-12 * C11
+
+
+# ---------------------------------------------------------------- stencil
+@pytest.mark.parametrize("shape", [(3, 4, 5), (6, 6, 6), (1, 2, 3), (7, 3, 2)])
+def test_apply_b_C_match_sparse_assembly(shape):
+    nx, ny, nz = shape
+    p, pix, rod, s = _rand_problem(nx, ny, nz, 4, seed=nx * 7 + ny)
+    o = O.Oracle(p, pix, rod).femat()
+    sm = R.SparseModel(nx, ny, nz, pix, o.cmod_array(), s)
+    x = np.random.default_rng(5).normal(size=3 * p.ns)
+    assert _rel(o.apply(x), sm.apply(x)) < 1e-13
+    assert _rel(o.b, sm.b) < 1e-13
+    assert abs(o.C - sm.C) <= 1e-12 * abs(sm.C)
+
+
+def test_rigid_translation_and_symmetry():
+    p, pix, rod, _ = _rand_problem(5, 4, 6, 5, seed=9)
+    o = O.Oracle(p, pix, rod).femat()
+    rng = np.random.default_rng(3)
+    v, w = rng.normal(size=3 * p.ns), rng.normal(size=3 * p.ns)
+    Kv, Kw = o.apply(v), o.apply(w)
+    assert abs(w @ Kv - v @ Kw) <= 1e-12 * np.linalg.norm(Kv) * np.linalg.norm(w)
+    for c in range(3):
+        t = np.zeros(3 * p.ns)
+        t[c * p.ns:(c + 1) * p.ns] = 1.0
+        assert np.linalg.norm(o.apply(t)) <= 1e-13 * np.linalg.norm(Kv) * np.sqrt(p.ns) / np.linalg.norm(v)
+
+
+def test_homogeneous_affine_is_equilibrium_and_energy_is_exact():
+    """One grain: the affine field is the exact solution, g = 0 and
+    U = 1/2 eps^T C eps * ns (engineering shear)."""
+    s = np.array([1e-3, -2e-4, 5e-4, 3e-4, -1e-4, 2e-4])  # exx eyy ezz exz eyz exy (tensor)
+    p = O.Problem(6, 5, 4, 2, exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5])
+    pix = np.ones(p.ns, np.int32)
+    rod = np.array([0.3, -0.2, 0.5])
+    o = O.Oracle(p, pix, rod).femat()
+    u = o.affine_u()
+    g, U = o.energy(u)
+    assert np.linalg.norm(g) <= 1e-10 * np.linalg.norm(o.b)
+    eng = np.array([s[0], s[1], s[2], 2 * s[3], 2 * s[4], 2 * s[5]])
+    Cm = o.cmod_array()[0]
+    assert abs(U - 0.5 * eng @ Cm @ eng * p.ns) <= 1e-10 * abs(U)
+    sig, eps = o.stress(u)
+    assert _rel(eps, eng) < 1e-12
+    assert _rel(sig, Cm @ eng) < 1e-12
+
+
+def test_invert3x3_rules():
+    rng = np.random.default_rng(4)
+    for _ in range(20):
+        A = rng.normal(size=(3, 3))
+        A = A @ A.T + 0.1 * np.eye(3)
+        assert np.abs(O.invert3x3(A) @ A - np.eye(3)).max() < 1e-10
+    assert np.abs(O.invert3x3(np.zeros((3, 3)))).max() == 0.0
+    assert np.abs(O.invert3x3(1e-6 * np.eye(3))).max() == 0.0  # |det| = 1e-18 < 1e-14
+
+
+def test_block_jacobi_matches_sparse_diagonal_blocks():
+    p, pix, rod, s = _rand_problem(4, 5, 3, 3, seed=11)
+    o = O.Oracle(p, pix, rod).femat()
+    minv = o.block_jacobi().reshape(3, 3, p.ns).transpose(2, 1, 0)
+    ref = R.SparseModel(4, 5, 3, pix, o.cmod_array(), s).block_jacobi()
+    assert np.abs(minv - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_pore_only_nodes_get_zero_preconditioner():
+    p = O.Problem(4, 4, 4, 3)
+    pix = np.full(p.ns, 3, np.int32)  # everything pore
+    pix[:8] = 1
+    rod = np.zeros(6)
+    o = O.Oracle(p, pix, rod).femat()
+    minv = o.block_jacobi().reshape(9, p.ns)
+    far = 42  # a node whose 8 elements are all pore
+    assert np.all(minv[:, far] == 0.0)
+
+
+# ---------------------------------------------------------------- solve
+def test_solve_matches_independent_pcg():
+    p, pix, rod, s = _rand_problem(6, 5, 7, 4, seed=21, strain=[1e-3, 0, 0, 0, 0, 0])
+    r = O.run(p, pix, rod)
+    o = O.Oracle(p, pix, rod).femat()
+    sm = R.SparseModel(p.nx, p.ny, p.nz, pix, o.cmod_array(), s)
+    u, L = sm.pcg(tol=p.tol)
+    assert abs(r["lstep"] - L) <= 2
+    _, U = sm.energy(u)
+    assert abs(r["utot"] - U) <= 1e-9 * abs(U)
+
+
+def test_effective_modulus_between_voigt_and_reuss():
+    rng = np.random.default_rng(8)
+    ng, n = 6, 8
+    p = O.Problem(n, n, n, ng + 1, c11=240e9, c12=150e9, c44=120e9, exx=1e-3, ezz=0.0, tol=1e-10)
+    # coarse random grains (2x2x2 blocks) with no pores
+    blocks = rng.integers(1, ng + 1, size=(n // 2,) * 3)
+    pix = np.repeat(np.repeat(np.repeat(blocks, 2, 0), 2, 1), 2, 2).transpose(2, 1, 0).ravel().astype(np.int32)
+    rod = rng.normal(size=3 * ng)
+    r = O.run(p, pix, rod)
+    o = O.Oracle(p, pix, rod).femat()
+    frac = np.bincount(pix, minlength=ng + 2)[1:ng + 1] / p.ns
+    Cs = o.cmod_array()[:ng]
+    Cv = np.einsum("g,gij->ij", frac, Cs)
+    Sr = np.einsum("g,gij->ij", frac, np.linalg.inv(Cs))
+    eps = np.array([1e-3, 0, 0, 0, 0, 0])
+    W = 0.5 * eps @ (r["strav"]) * 1.0  # energy density under the imposed strain
+    assert 0.5 * eps @ np.linalg.inv(Sr) @ eps <= W * (1 + 1e-9)
+    assert W <= 0.5 * eps @ Cv @ eps * (1 + 1e-9)
+    assert _rel(r["epsav"][[0]], [1e-3]) < 1e-9
+
+
+def test_divergence_reset_and_criterion_variants_run():
+    p, pix, rod, _ = _rand_problem(5, 5, 5, 3, seed=31, strain=[0, 0, 1e-3, 0, 0, 0])
+    for crit in (0, 1):
+        for reset in (0, 1):
+            p.criterion, p.divergence_reset = crit, reset
+            r = O.run(p, pix, rod)
+            assert r["exit_reason"] == 0 and r["lstep"] > 0
