@@ -60,6 +60,15 @@ struct e3d_handle {
   double* h1 = nullptr;
   double* Ah = nullptr;
   double* minv = nullptr;
+  // mixed precision (E3D_PREC_MIXED): FP32 inner-loop state
+  float* du32 = nullptr;
+  float* g32 = nullptr;
+  float* z32 = nullptr;
+  float* h32a = nullptr;
+  float* h32b = nullptr;
+  float* Ah32 = nullptr;
+  float* minv32 = nullptr;
+  int since_replace = 0;
   double* hx = nullptr;
   double* hy = nullptr;
   double* hd = nullptr;
@@ -75,6 +84,7 @@ struct e3d_handle {
   double gg0 = 0.0;
   bool uploaded = false, femat_done = false, energy_done = false, solve_ready = false, minv_ready = false;
   int pcg_grid = 0;
+  int pcg_grid32 = 0;
   double ms_setup = 0.0, ms_iter = 0.0;
   JumpParams J{};
 };
@@ -265,11 +275,17 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
   const int np = p->nphase;
   // PCG grid: as many co-resident tile blocks as the device holds.
   int per_sm = 0;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel, NT, 0)) != cudaSuccess)
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel<double>, NT, 0)) != cudaSuccess)
     return fail(cuda_fail(e, "occupancy"));
   if (per_sm < 1) return fail(E3D_ERR_CUDA);
   h->pcg_grid = per_sm * h->num_sms;
-  h->partial_n = std::max(h->pcg_grid, h->num_sms * 4) * 12;
+  int per_sm32 = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, pcg_persistent_kernel<float>, NT, 0)) !=
+      cudaSuccess)
+    return fail(cuda_fail(e, "occupancy"));
+  if (per_sm32 < 1) return fail(E3D_ERR_CUDA);
+  h->pcg_grid32 = per_sm32 * h->num_sms;
+  h->partial_n = std::max(std::max(h->pcg_grid, h->pcg_grid32), h->num_sms * 4) * 12;
   const long long halo = h->G.ntiles * h->G.tz;
   int32_t rc = E3D_OK;
   if ((rc = dalloc(h, &h->pix, ns)) || (rc = dalloc(h, &h->rod, 3 * (size_t)std::max(np - 1, 1))) ||
@@ -284,6 +300,15 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
       (rc = dalloc(h, &h->history, (size_t)std::max(p->max_iter, 1))) || (rc = dalloc(h, &h->st, 1)) ||
       (rc = dalloc(h, &h->bar, 1)) || (rc = dalloc(h, &h->err, 1)))
     return fail(rc);
+  if (p->precision == E3D_PREC_MIXED) {
+    if ((rc = dalloc(h, &h->du32, n3)) || (rc = dalloc(h, &h->g32, n3)) || (rc = dalloc(h, &h->z32, n3)) ||
+        (rc = dalloc(h, &h->h32a, n3)) || (rc = dalloc(h, &h->h32b, n3)) || (rc = dalloc(h, &h->Ah32, n3)) ||
+        (rc = dalloc(h, &h->minv32, 6 * ns)))
+      return fail(rc);
+    if ((e = cudaMemsetAsync(h->h32a, 0, sizeof(float) * n3, h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->h32b, 0, sizeof(float) * n3, h->stream)) != cudaSuccess)
+      return fail(cuda_fail(e, "memset"));
+  }
   if ((e = cudaMemsetAsync(h->err, 0, sizeof(int), h->stream)) != cudaSuccess) return fail(cuda_fail(e, "memset"));
   if ((e = cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream)) != cudaSuccess)
     return fail(cuda_fail(e, "memset"));
@@ -412,17 +437,27 @@ int32_t e3d_energy(e3d_handle_t* h, double* utot, double* gg) {
 int32_t e3d_solve_begin(e3d_handle_t* h) {
   if (!h) return E3D_ERR_INPUT;
   if (!h->energy_done) return E3D_ERR_STATE;
-  if (h->prob.precision != E3D_PREC_FP64) return E3D_ERR_INPUT;
+  const bool mixed = h->prob.precision == E3D_PREC_MIXED;
   cudaSetDevice(h->device);
   cudaEvent_t e0, e1;
   E3D_CUDA(cudaEventCreate(&e0));
   E3D_CUDA(cudaEventCreate(&e1));
   E3D_CUDA(cudaEventRecord(e0, h->stream));
-  // block-Jacobi (kkk == 1, src/elas3dxtal_pcg.f90:1498-1520)
-  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->pix, h->dkd, h->minv, nullptr);
+  // block-Jacobi (kkk == 1, src/elas3dxtal_pcg.f90:1498-1520); the mixed form
+  // keeps an FP32 copy of the FP64 inverse.
+  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->pix, h->dkd, h->minv,
+                                                                   mixed ? h->minv32 : nullptr);
   E3D_LAUNCHED(h);
   const int grid = reduction_grid(h);
-  pcg_init_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->minv, h->g, h->z, h->partial);
+  if (mixed) {
+    const long long n3 = 3 * h->G.ns;
+    to_float_kernel<<<blocks_for(n3, 256), 256, 0, h->stream>>>(n3, h->g, h->g32);
+    E3D_LAUNCHED(h);
+    E3D_CUDA(cudaMemsetAsync(h->du32, 0, sizeof(float) * n3, h->stream));
+    pcg_init_kernel<float><<<grid, 256, 0, h->stream>>>(h->G, h->minv32, h->g32, h->z32, h->partial);
+  } else {
+    pcg_init_kernel<double><<<grid, 256, 0, h->stream>>>(h->G, h->minv, h->g, h->z, h->partial);
+  }
   E3D_LAUNCHED(h);
   pcg_init_scalars_kernel<<<1, 256, 0, h->stream>>>(h->partial, grid, h->gg0, h->prob.criterion, h->prob.tol,
                                                     h->prob.max_iter, h->prob.divergence_reset, h->st);
@@ -436,6 +471,7 @@ int32_t e3d_solve_begin(e3d_handle_t* h) {
   if (rc) return rc;
   h->ms_setup = ms;
   h->ms_iter = 0.0;
+  h->since_replace = 0;
   h->minv_ready = true;
   h->solve_ready = true;
   return E3D_OK;
@@ -459,7 +495,7 @@ static int32_t fill_stats(e3d_handle* h, e3d_solve_stats_t* st, int32_t* exit_re
     st->iterations = S.it;
     st->exit_reason = reason;
     st->resets = S.resets;
-    st->refinements = 0;
+    st->refinements = S.refinements;
     st->gg = S.gg;
     st->gg0 = S.gg0;
     st->rel_res = S.rel_res;
@@ -470,11 +506,16 @@ static int32_t fill_stats(e3d_handle* h, e3d_solve_stats_t* st, int32_t* exit_re
   return E3D_OK;
 }
 
-int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
-  if (!h || n < 0) return E3D_ERR_INPUT;
-  if (!h->solve_ready) return E3D_ERR_STATE;
-  cudaSetDevice(h->device);
-  PcgArgs P{};
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+PcgArgs<T> pcg_args(e3d_handle* h);
+
+template <>
+PcgArgs<double> pcg_args<double>(e3d_handle* h) {
+  PcgArgs<double> P{};
   P.A = apply_args(h, nullptr, h->Ah);
   P.h0 = h->h0;
   P.h1 = h->h1;
@@ -483,44 +524,118 @@ int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
   P.z = h->z;
   P.Ah = h->Ah;
   P.minv = h->minv;
+  return P;
+}
+
+template <>
+PcgArgs<float> pcg_args<float>(e3d_handle* h) {
+  PcgArgs<float> P{};
+  P.A.g = h->G;
+  P.A.pix = h->pix;
+  P.A.cs = h->cs32;
+  P.A.hx = reinterpret_cast<float*>(h->hx);  // the FP64 halo buffers, reused
+  P.A.hy = reinterpret_cast<float*>(h->hy);
+  P.A.hd = reinterpret_cast<float*>(h->hd);
+  P.A.y = h->Ah32;
+  P.h0 = h->h32a;
+  P.h1 = h->h32b;
+  P.u = h->du32;
+  P.g = h->g32;
+  P.z = h->z32;
+  P.Ah = h->Ah32;
+  P.minv = h->minv32;
+  return P;
+}
+
+template <typename T>
+int32_t launch_pcg(e3d_handle* h, int it_limit, int grid) {
+  PcgArgs<T> P = pcg_args<T>(h);
   P.partA = h->partial;
-  P.partB = h->partial + h->pcg_grid;
+  P.partB = h->partial + grid;
   P.st = h->st;
   P.history = h->history;
   P.bar = h->bar;
   P.err = h->err;
   P.timeout_ns = 60ull * 1000000000ull;
+  P.it_limit = it_limit;
   E3D_CUDA(cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream));
+  void* args[] = {&P};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)pcg_persistent_kernel<T>, dim3(grid), dim3(NT), args,
+                                              0, h->stream);
+  h->launches++;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(pcg)");
+  return E3D_OK;
+}
+
+int32_t read_state(e3d_handle* h, PcgState* S) {
+  E3D_CUDA(cudaMemcpyAsync(S, h->st, sizeof *S, cudaMemcpyDeviceToHost, h->stream));
+  E3D_CUDA(cudaStreamSynchronize(h->stream));
+  return E3D_OK;
+}
+
+// Mixed form: fold the FP32 correction into u (FP64).
+int32_t fold_correction(e3d_handle* h) {
+  const long long n3 = 3 * h->G.ns;
+  fold_correction_kernel<<<blocks_for(n3, 256), 256, 0, h->stream>>>(n3, h->du32, h->u, h->du32);
+  E3D_LAUNCHED(h);
+  return E3D_OK;
+}
+
+// Mixed form: FP64 residual replacement -- fold du into u, recompute the true
+// gradient g = K u + b with the FP64 stencil, and restart the FP32 recurrence
+// from it (z = Minv32 g, gg = z.g accumulated in FP64).
+int32_t residual_replacement(e3d_handle* h) {
+  int32_t rc = fold_correction(h);
+  if (rc) return rc;
+  if ((rc = launch_apply_tiles(h, h->u, h->Ah))) return rc;
+  const int grid = reduction_grid(h);
+  true_residual_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->Ah, h->hx, h->hy, h->hd, h->b, h->minv32, h->g,
+                                                    h->g32, h->z32, h->partial);
+  E3D_LAUNCHED(h);
+  replace_scalars_kernel<<<1, 256, 0, h->stream>>>(h->partial, grid, h->st, h->history);
+  E3D_LAUNCHED(h);
+  h->since_replace = 0;
+  return E3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
+  if (!h || n < 0) return E3D_ERR_INPUT;
+  if (!h->solve_ready) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const bool mixed = h->prob.precision == E3D_PREC_MIXED;
+  const int R = h->prob.refine_every > 0 ? h->prob.refine_every : 50;
   cudaEvent_t e0, e1;
   E3D_CUDA(cudaEventCreate(&e0));
   E3D_CUDA(cudaEventCreate(&e1));
   E3D_CUDA(cudaEventRecord(e0, h->stream));
-  // Chunks of iterations per cooperative launch keep single launches short.
+  // Chunks of iterations per cooperative launch keep single launches short;
+  // the mixed form also ends a chunk at every residual replacement.
   int remaining = n;
   int32_t rc = E3D_OK;
+  PcgState S{};
   while (remaining > 0) {
-    const int chunk = std::min(remaining, 256);
-    P.it_limit = chunk;
-    void* args[] = {&P};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)pcg_persistent_kernel, dim3(h->pcg_grid), dim3(NT),
-                                                args, 0, h->stream);
-    h->launches++;
-    if (e != cudaSuccess) {
-      rc = cuda_fail(e, "cudaLaunchCooperativeKernel(pcg)");
-      break;
-    }
+    int chunk = std::min(remaining, 256);
+    if (mixed) chunk = std::min(chunk, R - h->since_replace);
+    rc = mixed ? launch_pcg<float>(h, chunk, h->pcg_grid32) : launch_pcg<double>(h, chunk, h->pcg_grid);
+    if (rc) break;
+    if ((rc = read_state(h, &S))) break;
+    const int done = S.it;  // iterations so far
+    (void)done;
     remaining -= chunk;
-    if (remaining > 0) {
-      PcgState S{};
-      e = cudaMemcpyAsync(&S, h->st, sizeof S, cudaMemcpyDeviceToHost, h->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-      if (e != cudaSuccess) {
-        rc = cuda_fail(e, "pcg state");
-        break;
+    if (mixed) {
+      h->since_replace += chunk;
+      if (S.status == PCG_CONVERGED || (S.status == PCG_RUNNING && h->since_replace >= R)) {
+        if ((rc = residual_replacement(h))) break;
+        if ((rc = read_state(h, &S))) break;
       }
-      if (S.status != PCG_RUNNING) break;
     }
+    if (S.status != PCG_RUNNING) break;
   }
+  if (!rc && mixed) rc = fold_correction(h);  // u always holds the current iterate on return
   cudaEventRecord(e1, h->stream);
   int32_t rs = sync(h);
   float ms = 0.f;

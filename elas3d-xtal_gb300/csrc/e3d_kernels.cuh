@@ -16,6 +16,17 @@ namespace e3d {
 
 constexpr int TILE_X = 32;
 constexpr int TILE_Y = 8;
+
+// Tuning knobs of the persistent PCG kernel (set at build time).
+#ifndef E3D_PB_UNROLL_F32
+#define E3D_PB_UNROLL_F32 2  // phase-B nodes in flight per thread, FP32 form
+#endif
+#ifndef E3D_PB_UNROLL_F64
+#define E3D_PB_UNROLL_F64 1  // phase-B nodes in flight per thread, FP64 form
+#endif
+#ifndef E3D_F32_BLOCKS_PER_SM
+#define E3D_F32_BLOCKS_PER_SM 2  // resident 256-thread blocks per SM, FP32 form
+#endif
 constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
 
 // Device status codes (host maps them to E3D_*).
@@ -98,26 +109,48 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   }
   const int hgx = wrapi(x0 + hlx, G.nx), hgy = wrapi(y0 + hly, G.ny);
 
-  auto fetch = [&](long long m, T (&v)[3]) {
+  // Raw loads of one node plane are issued a step ahead (prefetch) so they are
+  // in flight while the previous element computes; commit forms h_new and
+  // stores the plane into shared memory.
+  T pz_own[3], px_own[3], pz_h[3], px_h[3];
+  const bool need_x = !FUSED || !A.reset;
+  auto prefetch = [&](int zl) {
+    const int zp = wrapi(zl, G.nz);
+    if (active) {
+      const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (FUSED) {
-        const T zz = __ldcg(A.zv + m + c * ns);
-        v[c] = A.reset ? zz : fma_(A.gamma, __ldcg(A.x + m + c * ns), zz);
-      } else {
-        v[c] = __ldcg(A.x + m + c * ns);
+      for (int c = 0; c < 3; ++c) {
+        if (need_x) px_own[c] = __ldcg(A.x + m + c * ns);
+        if (FUSED) pz_own[c] = __ldcg(A.zv + m + c * ns);
+      }
+    }
+    if (tid < nhalo) {
+      const long long m = (long long)hgx + (long long)G.nx * hgy + nxy * zp;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (need_x) px_h[c] = __ldcg(A.x + m + c * ns);
+        if (FUSED) pz_h[c] = __ldcg(A.zv + m + c * ns);
       }
     }
   };
-  auto load_plane = [&](int zl, bool own) {
+  auto combine = [&](const T (&zz)[3], const T (&xx)[3], T (&v)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (FUSED)
+        v[c] = A.reset ? zz[c] : fma_(A.gamma, xx[c], zz[c]);
+      else
+        v[c] = xx[c];
+    }
+  };
+  auto commit = [&](int zl, bool own) {
     const int zp = wrapi(zl, G.nz);
     T* buf0 = sm.node[(zl + 2) & 1][0];
     const int stride = (TILE_X + 1) * (TILE_Y + 1);
     if (active) {
-      const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
       T v[3];
-      fetch(m, v);
+      combine(pz_own, px_own, v);
       if (FUSED && own) {
+        const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
 #pragma unroll
         for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = v[c];
       }
@@ -125,9 +158,8 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       for (int c = 0; c < 3; ++c) buf0[c * stride + ty * (TILE_X + 1) + tx] = v[c];
     }
     if (tid < nhalo) {
-      const long long m = (long long)hgx + (long long)G.nx * hgy + nxy * zp;
       T v[3];
-      fetch(m, v);
+      combine(pz_h, px_h, v);
 #pragma unroll
       for (int c = 0; c < 3; ++c) buf0[c * stride + hly * (TILE_X + 1) + hlx] = v[c];
     }
@@ -146,18 +178,24 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   };
 
   T cur[3][4], Pold[3][4], carry[3][4];
-  load_plane(z0 - 1, false);
+  const long long ecol = (long long)xg + (long long)G.nx * yg;  // element column
+  prefetch(z0 - 1);
+  commit(z0 - 1, false);
   __syncthreads();
   if (active) {
     read_corners(z0 - 1, cur);
 #pragma unroll
     for (int c = 0; c < 3; ++c) had_xy(cur[c], Pold[c]);
   }
+  prefetch(z0);
+  int ph_cur = active ? __ldg(A.pix + ecol + nxy * wrapi(z0 - 1, G.nz)) : 0;
   const int htiles_stride = G.tz;  // per-tile plane stride in halo buffers
   for (int k = z0 - 1; k < z0 + wz; ++k) {
     const bool own_next = (k + 1 >= z0) && (k + 1 < z0 + wz);
-    load_plane(k + 1, own_next);
+    commit(k + 1, own_next);
     __syncthreads();
+    if (k + 2 <= z0 + wz) prefetch(k + 2);
+    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldg(A.pix + ecol + nxy * wrapi(k + 1, G.nz)) : 0;
     T rr[3][4];
     T nxt[3][4];
     if (active) {
@@ -173,10 +211,8 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
           h[c][b + 4] = Pn[c][b] - Pold[c][b];
         }
       }
-      const int zp = wrapi(k, G.nz);
-      const int ph = __ldg(A.pix + (long long)xg + (long long)G.nx * yg + nxy * zp);
       T f[3][8];
-      element_modal<T>(A.cs + (long long)ph * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
+      element_modal<T>(A.cs + (long long)ph_cur * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         T lo[4];
@@ -205,39 +241,34 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       if (active) {
         const int lz = k - z0;
         const long long m = (long long)xg + (long long)G.nx * yg + nxy * wrapi(k, G.nz);
-        T hxv[3], hyv[3];
+        T hxv[3], hyv[3], acc[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          T acc = rr[c][0];
-          if (tx > 0) acc += sm.r[3 * c + 0][tid - 1];
-          if (ty > 0) acc += sm.r[3 * c + 1][tid - TILE_X];
-          if (tx > 0 && ty > 0) acc += sm.r[3 * c + 2][tid - TILE_X - 1];
-          A.y[m + c * ns] = acc;
-          hAh += (double)cur[c][0] * (double)acc;
+          acc[c] = rr[c][0];
+          if (tx > 0) acc[c] += sm.r[3 * c + 0][tid - 1];
+          if (ty > 0) acc[c] += sm.r[3 * c + 1][tid - TILE_X];
+          if (tx > 0 && ty > 0) acc[c] += sm.r[3 * c + 2][tid - TILE_X - 1];
+          A.y[m + c * ns] = acc[c];
           hxv[c] = rr[c][1] + (ty > 0 ? sm.r[3 * c + 2][tid - TILE_X] : T(0));
           hyv[c] = rr[c][2] + (tx > 0 ? sm.r[3 * c + 2][tid - 1] : T(0));
         }
+        // per-node dot in T, accumulated in FP64
+        hAh += (double)(cur[0][0] * acc[0] + cur[1][0] * acc[1] + cur[2][0] * acc[2]);
         const long long hb = tile * htiles_stride + lz;
         if (tx == wx - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            A.hx[((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty] = hxv[c];
-            hAh += (double)cur[c][1] * (double)hxv[c];
-          }
+          for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty] = hxv[c];
+          hAh += (double)(cur[0][1] * hxv[0] + cur[1][1] * hxv[1] + cur[2][1] * hxv[2]);
         }
         if (ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            A.hy[((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx] = hyv[c];
-            hAh += (double)cur[c][2] * (double)hyv[c];
-          }
+          for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx] = hyv[c];
+          hAh += (double)(cur[0][2] * hyv[0] + cur[1][2] * hyv[1] + cur[2][2] * hyv[2]);
         }
         if (tx == wx - 1 && ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            A.hd[(long long)c * G.ntiles * htiles_stride + hb] = rr[c][3];
-            hAh += (double)cur[c][3] * (double)rr[c][3];
-          }
+          for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * htiles_stride + hb] = rr[c][3];
+          hAh += (double)(cur[0][3] * rr[0][3] + cur[1][3] * rr[1][3] + cur[2][3] * rr[2][3]);
         }
       }
     }
@@ -247,6 +278,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
 #pragma unroll
         for (int b = 0; b < 4; ++b) cur[c][b] = nxt[c][b];
     }
+    ph_cur = ph_nxt;
   }
 }
 
@@ -258,6 +290,34 @@ __device__ __forceinline__ void halo_add(const GridDims& G, const T* __restrict_
   const int tix = x / TILE_X, lx = x - tix * TILE_X;
   const int tiy = y / TILE_Y, ly = y - tiy * TILE_Y;
   const int tiz = z / G.tz, lz = z - tiz * G.tz;
+  if (lx != 0 && ly != 0) return;
+  const int txl = tix == 0 ? G.ntx - 1 : tix - 1;
+  const int tyd = tiy == 0 ? G.nty - 1 : tiy - 1;
+  const long long plane = (long long)tiz * G.nty;
+  const long long per_c = G.ntiles * G.tz;
+  if (lx == 0) {
+    const long long t = (long long)txl + (long long)G.ntx * (tiy + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + (c * per_c + t * G.tz + lz) * TILE_Y + ly);
+  }
+  if (ly == 0) {
+    const long long t = (long long)tix + (long long)G.ntx * (tyd + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + (c * per_c + t * G.tz + lz) * TILE_X + lx);
+  }
+  if (lx == 0 && ly == 0) {
+    const long long t = (long long)txl + (long long)G.ntx * (tyd + plane);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + c * per_c + t * G.tz + lz);
+  }
+}
+
+// halo_add for a node whose tile coordinates are known (no integer division);
+// same additions in the same order.
+template <typename T>
+__device__ __forceinline__ void halo_add_tile(const GridDims& G, const T* __restrict__ hx,
+                                              const T* __restrict__ hy, const T* __restrict__ hd,
+                                              int tix, int tiy, int tiz, int lx, int ly, int lz, T (&v)[3]) {
   if (lx != 0 && ly != 0) return;
   const int txl = tix == 0 ? G.ntx - 1 : tix - 1;
   const int tyd = tiy == 0 ? G.nty - 1 : tiy - 1;
@@ -669,7 +729,7 @@ __global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pix, cons
   invert3x3(M, Mi);
   const double s[6] = {Mi[0][0], Mi[1][1], Mi[2][2], Mi[0][1], Mi[0][2], Mi[1][2]};
   for (int q = 0; q < 6; ++q) {
-    minv[m + q * G.ns] = s[q];
+    if (minv) minv[m + q * G.ns] = s[q];
     if (minv32) minv32[m + q * G.ns] = (float)s[q];
   }
 }
@@ -792,8 +852,8 @@ __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32_t* __r
 //   B: u -= lambda h ; g -= lambda Ah ; z = Minv g ; partial z.g     | barrier
 //      rel_res, divergence reset (:1961-1981), gamma (:1988), stop test (:2007)
 struct PcgState {
-  double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, pad;
-  int it, status, reset, resets, cur, max_iter, divergence_reset, pad2;
+  double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
+  int it, status, reset, resets, cur, max_iter, divergence_reset, refinements;
 };
 
 struct GridBarrier {
@@ -853,15 +913,20 @@ __device__ double reduce_broadcast(const double* partial, int n, double* red) {
   return s_val;
 }
 
+// T = double: the plain FP64 solve (u is the solution).  T = float: the inner
+// loop of the mixed-precision solve (u is the FP32 correction since the last
+// FP64 residual replacement; stencil, preconditioner and vectors in FP32, dot
+// products and scalar recurrences in FP64).
+template <typename T>
 struct PcgArgs {
-  ApplyArgs<double> A;  // x / hnew / zv / gamma / reset set per iteration
-  double* h0;
-  double* h1;
-  double* u;
-  double* g;
-  double* z;
-  double* Ah;
-  const double* minv;
+  ApplyArgs<T> A;  // x / hnew / zv / gamma / reset set per iteration
+  T* h0;
+  T* h1;
+  T* u;
+  T* g;
+  T* z;
+  T* Ah;
+  const T* minv;
   double* partA;  // [gridDim.x]
   double* partB;  // [gridDim.x]
   PcgState* st;
@@ -872,8 +937,9 @@ struct PcgArgs {
   unsigned long long timeout_ns;
 };
 
-__global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
-  __shared__ ApplySmem<double> sm;
+template <typename T>
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1) pcg_persistent_kernel(PcgArgs<T> P) {
+  __shared__ ApplySmem<T> sm;
   __shared__ double red[NT / 32];
   __shared__ PcgState S0;
   if (threadIdx.x == 0) S0 = *P.st;
@@ -885,16 +951,16 @@ __global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
   const int it_end = min(s.it + P.it_limit, s.max_iter);
   while (s.it < it_end) {
     // ---- phase A: fused direction update + stencil + h.Ah
-    ApplyArgs<double> A = P.A;
+    ApplyArgs<T> A = P.A;
     A.x = s.cur ? P.h1 : P.h0;
     A.hnew = s.cur ? P.h0 : P.h1;
     A.zv = P.z;
     A.y = P.Ah;
-    A.gamma = s.gamma;
+    A.gamma = (T)s.gamma;
     A.reset = s.reset;
     double hAh_t = 0.0;
     for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
-      apply_tile<double, true>(A, t, sm, hAh_t);
+      apply_tile<T, true>(A, t, sm, hAh_t);
       __syncthreads();
     }
     {
@@ -918,30 +984,62 @@ __global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
       break;
     }
     const double lambda = s.gg / hAh;
-    // ---- phase B: u, g update, preconditioner, z.g
-    const double* hc = s.cur ? P.h1 : P.h0;
+    const T lam = (T)lambda;
+    // ---- phase B: u, g update, preconditioner, z.g -- node loop in tile order
+    // (no index division), z unrolled so several nodes' loads are in flight.
+    const T* hc = s.cur ? P.h1 : P.h0;
     double zg_t = 0.0;
-    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < ns;
-         m += (long long)gridDim.x * blockDim.x) {
-      const int x = (int)(m % G.nx);
-      const int y = (int)((m / G.nx) % G.ny);
-      const int zc = (int)(m / ((long long)G.nx * G.ny));
-      double ah[3] = {__ldcg(P.Ah + m), __ldcg(P.Ah + m + ns), __ldcg(P.Ah + m + 2 * ns)};
-      halo_add<double>(G, P.A.hx, P.A.hy, P.A.hd, x, y, zc, ah);
-      double gv[3];
+    {
+      constexpr int U = sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64;
+      const int tx = threadIdx.x % TILE_X, ty = threadIdx.x / TILE_X;
+      const long long nxy = (long long)G.nx * G.ny;
+      for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
+        const int tix = (int)(t % G.ntx);
+        const int tiy = (int)((t / G.ntx) % G.nty);
+        const int tiz = (int)(t / ((long long)G.ntx * G.nty));
+        const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+        const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+        if (tx >= wx || ty >= wy) continue;
+        const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+        for (int lz0 = 0; lz0 < wz; lz0 += U) {
+          T ah[U][3], hv[U][3], uv[U][3], gv[U][3], mi[U][6];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const long long i = m + c * ns;
-        P.u[i] = P.u[i] - lambda * __ldcg(hc + i);
-        gv[c] = P.g[i] - lambda * ah[c];
-        P.g[i] = gv[c];
-      }
-      double zv[3];
-      precond3<double>(P.minv, m, ns, gv, zv);
+          for (int j = 0; j < U; ++j) {
+            if (lz0 + j < wz) {
+              const long long m = col + nxy * (z0 + lz0 + j);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        P.z[m + c * ns] = zv[c];
-        zg_t += zv[c] * gv[c];
+              for (int c = 0; c < 3; ++c) {
+                ah[j][c] = __ldcg(P.Ah + m + c * ns);
+                hv[j][c] = __ldcg(hc + m + c * ns);
+                uv[j][c] = P.u[m + c * ns];
+                gv[j][c] = P.g[m + c * ns];
+              }
+#pragma unroll
+              for (int q = 0; q < 6; ++q) mi[j][q] = __ldg(P.minv + m + q * ns);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < U; ++j) {
+            if (lz0 + j < wz) {
+              const long long m = col + nxy * (z0 + lz0 + j);
+              halo_add_tile<T>(G, P.A.hx, P.A.hy, P.A.hd, tix, tiy, tiz, tx, ty, lz0 + j, ah[j]);
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                P.u[m + c * ns] = uv[j][c] - lam * hv[j][c];
+                gv[j][c] = gv[j][c] - lam * ah[j][c];
+                P.g[m + c * ns] = gv[j][c];
+              }
+              // z = Minv g (src/elas3dxtal_pcg.f90:1930-1932), symmetric Minv
+              const T z0v = mi[j][0] * gv[j][0] + mi[j][3] * gv[j][1] + mi[j][4] * gv[j][2];
+              const T z1v = mi[j][3] * gv[j][0] + mi[j][1] * gv[j][1] + mi[j][5] * gv[j][2];
+              const T z2v = mi[j][4] * gv[j][0] + mi[j][5] * gv[j][1] + mi[j][2] * gv[j][2];
+              P.z[m] = z0v;
+              P.z[m + ns] = z1v;
+              P.z[m + 2 * ns] = z2v;
+              zg_t += (double)(z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2]);
+            }
+          }
+        }
       }
     }
     {
@@ -954,6 +1052,7 @@ __global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
     }
     const double gglast = s.gg;
     s.gg = reduce_broadcast(P.partB, gridDim.x, red);
+    s.gglast = gglast;
     if (!isfinite(s.gg)) {
       s.status = PCG_BREAKDOWN;
       break;
@@ -979,19 +1078,20 @@ __global__ void __launch_bounds__(NT, 1) pcg_persistent_kernel(PcgArgs P) {
 }
 
 // PCG set-up (src/elas3dxtal_pcg.f90:1527-1567): z = Minv g, partial z.g.
-__global__ void __launch_bounds__(256) pcg_init_kernel(GridDims G, const double* __restrict__ minv,
-                                                       const double* __restrict__ g, double* __restrict__ z,
+template <typename T>
+__global__ void __launch_bounds__(256) pcg_init_kernel(GridDims G, const T* __restrict__ minv,
+                                                       const T* __restrict__ g, T* __restrict__ z,
                                                        double* partial) {
   __shared__ double red[8];
   double acc = 0.0;
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
        m += (long long)gridDim.x * blockDim.x) {
-    const double gv[3] = {g[m], g[m + G.ns], g[m + 2 * G.ns]};
-    double zv[3];
-    precond3<double>(minv, m, G.ns, gv, zv);
+    const T gv[3] = {g[m], g[m + G.ns], g[m + 2 * G.ns]};
+    T zv[3];
+    precond3<T>(minv, m, G.ns, gv, zv);
     for (int c = 0; c < 3; ++c) {
       z[m + c * G.ns] = zv[c];
-      acc += zv[c] * gv[c];
+      acc += (double)zv[c] * (double)gv[c];
     }
   }
   const double s = block_sum<256>(acc, red);
@@ -1014,7 +1114,7 @@ __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int 
     S.gamma = 0.0;
     S.tol = (double)tol;
     S.hAh = 0.0;
-    S.pad = 0.0;
+    S.gglast = gg;
     S.it = 0;
     S.status = PCG_RUNNING;
     S.reset = 1;  // h = z on the first step (:1554-1562)
@@ -1022,9 +1122,93 @@ __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int 
     S.cur = 0;
     S.max_iter = max_iter;
     S.divergence_reset = divergence_reset;
-    S.pad2 = 0;
+    S.refinements = 0;
     *st = S;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP64 residual replacement between FP32 inner chunks.
+// u64 += du32 ; du32 = 0 (the inner loop restarts its correction at zero).
+__global__ void fold_correction_kernel(long long n3, const float* __restrict__ du, double* __restrict__ u,
+                                       float* __restrict__ du_zero) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  u[i] += (double)du[i];
+  du_zero[i] = 0.0f;
+}
+
+// g = K u + b from the FP64 stencil (in-tile part + halos), stored in FP64 and
+// FP32; then z32 = Minv32 g32 and partial z.g for the replaced residual.
+__global__ void __launch_bounds__(256) true_residual_kernel(GridDims G, const double* __restrict__ ku,
+                                                            const double* __restrict__ hx,
+                                                            const double* __restrict__ hy,
+                                                            const double* __restrict__ hd,
+                                                            const double* __restrict__ b, const float* __restrict__ minv32,
+                                                            double* __restrict__ g64, float* __restrict__ g32,
+                                                            float* __restrict__ z32, double* partial) {
+  __shared__ double red[8];
+  double acc = 0.0;
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
+       m += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(m % G.nx);
+    const int y = (int)((m / G.nx) % G.ny);
+    const int z = (int)(m / ((long long)G.nx * G.ny));
+    double v[3] = {ku[m], ku[m + G.ns], ku[m + 2 * G.ns]};
+    halo_add<double>(G, hx, hy, hd, x, y, z, v);
+    float gv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long i = m + c * G.ns;
+      const double gd = v[c] + b[i];
+      g64[i] = gd;
+      gv[c] = (float)gd;
+      g32[i] = gv[c];
+    }
+    float zv[3];
+    precond3<float>(minv32, m, G.ns, gv, zv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      z32[m + c * G.ns] = zv[c];
+      acc += (double)zv[c] * (double)gv[c];
+    }
+  }
+  const double s = block_sum<256>(acc, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Scalars after a residual replacement: gg from the true residual, gamma
+// re-derived from it (the direction h is kept), and a convergence flag that
+// only stands if the true residual also meets the tolerance.
+__global__ void replace_scalars_kernel(const double* __restrict__ partial, int n, PcgState* st,
+                                       double* history) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  const double gg = block_sum<256>(s, red);
+  if (threadIdx.x == 0) {
+    PcgState S = *st;
+    S.gg = gg;
+    S.refinements += 1;
+    if (!isfinite(gg)) {
+      S.status = PCG_BREAKDOWN;
+    } else {
+      const double rel = sqrt(gg / S.gg0);
+      S.rel_res = rel;
+      S.rel_res_prev = rel;
+      if (!S.reset) S.gamma = gg / S.gglast;
+      if (history && S.it > 0) history[S.it - 1] = rel;
+      if (S.status == PCG_CONVERGED && !(rel < S.tol)) S.status = PCG_RUNNING;
+      if (S.status == PCG_RUNNING && rel < S.tol) S.status = PCG_CONVERGED;
+    }
+    *st = S;
+  }
+}
+
+// g32 = (float) g64 at the start of a mixed solve.
+__global__ void to_float_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 }  // namespace e3d
