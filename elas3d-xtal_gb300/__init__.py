@@ -435,3 +435,194 @@ def euler_to_rodrigues(euler: np.ndarray) -> np.ndarray:
     out = np.empty_like(e)
     load_library().e3d_euler_to_rodrigues(e.size // 3, _dp(e), _dp(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Batched ensembles and the serving loop (include/e3d_batch.h)
+class RveC(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("ngrains", C.c_int32),
+                ("c11", C.c_double), ("c12", C.c_double), ("c44", C.c_double),
+                ("pix", C.POINTER(C.c_int32)), ("rodrigues", C.POINTER(C.c_double))]
+
+
+class BatchOptsC(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_iter", C.c_int32), ("refine_every", C.c_int32),
+                ("criterion", C.c_int32), ("divergence_reset", C.c_int32), ("tol", C.c_float),
+                ("load_cases", C.c_int32), ("parts", C.c_int32), ("pad", C.c_int32),
+                ("strain", C.c_double), ("e1", C.c_double), ("nu1", C.c_double), ("hbm_budget", C.c_int64)]
+
+
+class JobResultC(C.Structure):
+    _fields_ = [("rve", C.c_int32), ("load_case", C.c_int32), ("status", C.c_int32),
+                ("iterations", C.c_int32), ("refinements", C.c_int32), ("resets", C.c_int32),
+                ("parts", C.c_int32), ("pad", C.c_int32), ("utot0", C.c_double), ("utot", C.c_double),
+                ("rel_res", C.c_double), ("true_rel", C.c_double), ("strav", C.c_double * 6),
+                ("epsav", C.c_double * 6), ("seconds", C.c_double)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("strav", "epsav", "pad")}
+        d["strav"] = np.array(self.strav[:])
+        d["epsav"] = np.array(self.epsav[:])
+        return d
+
+
+class ServeOptsC(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_iter", C.c_int32), ("refine_every", C.c_int32),
+                ("criterion", C.c_int32), ("divergence_reset", C.c_int32), ("tol", C.c_float),
+                ("max_active", C.c_int32), ("round_iters", C.c_int32), ("parts", C.c_int32),
+                ("pad", C.c_int32), ("e1", C.c_double), ("nu1", C.c_double), ("hbm_budget", C.c_int64)]
+
+
+BATCH_SYMBOLS = ("e3d_batch_opts_defaults", "e3d_batch_create", "e3d_batch_solve", "e3d_batch_results",
+                 "e3d_batch_parts", "e3d_batch_destroy", "e3d_serve_opts_defaults", "e3d_serve_create",
+                 "e3d_serve_submit", "e3d_serve_step", "e3d_serve_result", "e3d_serve_memory",
+                 "e3d_serve_destroy")
+EXPORTED_SYMBOLS = EXPORTED_SYMBOLS + BATCH_SYMBOLS
+
+
+def _bind_batch(L):
+    if getattr(L, "_e3d_batch_bound", False):
+        return L
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    L.e3d_batch_opts_defaults.argtypes = [C.POINTER(BatchOptsC)]
+    L.e3d_batch_opts_defaults.restype = None
+    L.e3d_batch_create.argtypes = [C.POINTER(vp), C.POINTER(RveC), C.c_int32, C.POINTER(BatchOptsC)]
+    L.e3d_batch_solve.argtypes = [vp, dp, dp]
+    L.e3d_batch_results.argtypes = [vp, C.POINTER(JobResultC), C.c_int32, ip]
+    L.e3d_batch_parts.argtypes = [vp, ip, C.c_int32]
+    L.e3d_batch_destroy.argtypes = [vp]
+    L.e3d_serve_opts_defaults.argtypes = [C.POINTER(ServeOptsC)]
+    L.e3d_serve_opts_defaults.restype = None
+    L.e3d_serve_create.argtypes = [C.POINTER(vp), C.POINTER(ServeOptsC)]
+    L.e3d_serve_submit.argtypes = [vp, C.POINTER(RveC), dp, C.POINTER(C.c_int64)]
+    L.e3d_serve_step.argtypes = [vp, ip]
+    L.e3d_serve_result.argtypes = [vp, C.c_int64, C.POINTER(JobResultC)]
+    L.e3d_serve_memory.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.e3d_serve_destroy.argtypes = [vp]
+    L._e3d_batch_bound = True
+    return L
+
+
+def _rve_struct(rve: dict, keep: list) -> RveC:
+    pix = np.ascontiguousarray(rve["pix"], dtype=np.int32).reshape(-1)
+    rod = np.ascontiguousarray(rve["rodrigues"], dtype=np.float64).reshape(-1)
+    keep += [pix, rod]
+    nx, ny, nz = rve["shape"]
+    return RveC(nx, ny, nz, int(rve["ngrains"]), float(rve["c11"]), float(rve["c12"]), float(rve["c44"]),
+                _ip(pix), _dp(rod))
+
+
+class Batch:
+    """Many RVEs x the six unit load cases in one persistent launch (CUDA graph).
+
+    rves: list of dicts with keys shape (nx,ny,nz), ngrains, c11, c12, c44,
+    pix (1-based phase ids), rodrigues (3*ngrains)."""
+
+    def __init__(self, rves, *, max_iter=10000, refine_every=50, tol=1e-8, criterion=CRIT_REF,
+                 load_cases=0, parts=0, strain=1e-3, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
+        self.L = _bind_batch(load_library())
+        o = BatchOptsC()
+        self.L.e3d_batch_opts_defaults(C.byref(o))
+        o.device, o.max_iter, o.refine_every, o.tol, o.criterion = device, max_iter, refine_every, tol, criterion
+        o.load_cases, o.parts, o.strain, o.e1, o.nu1, o.hbm_budget = load_cases, parts, strain, e1, nu1, hbm_budget
+        keep = []
+        arr = (RveC * len(rves))(*[_rve_struct(r, keep) for r in rves])
+        self.n = len(rves)
+        self.ncases = bin(load_cases or 0x3F).count("1")
+        self._h = C.c_void_p()
+        _check(self.L.e3d_batch_create(C.byref(self._h), arr, len(rves), C.byref(o)), "e3d_batch_create")
+
+    def solve(self):
+        ceff = np.zeros(36 * self.n)
+        sec = C.c_double()
+        rc = self.L.e3d_batch_solve(self._h, _dp(ceff), C.byref(sec))
+        _check(rc, "e3d_batch_solve", allow=(E3D_ERR_MAXITER,))
+        return ceff.reshape(self.n, 6, 6), sec.value
+
+    def results(self):
+        nj = self.n * self.ncases
+        out = (JobResultC * nj)()
+        cnt = C.c_int32()
+        _check(self.L.e3d_batch_results(self._h, out, nj, C.byref(cnt)), "e3d_batch_results")
+        return [r.as_dict() for r in out[: cnt.value]]
+
+    def parts(self):
+        nj = self.n * self.ncases
+        arr = np.zeros(nj, np.int32)
+        _check(self.L.e3d_batch_parts(self._h, _ip(arr), nj), "e3d_batch_parts")
+        return arr
+
+    def close(self):
+        if self._h:
+            self.L.e3d_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching solve server (admission by slots and HBM budget)."""
+
+    def __init__(self, *, max_active=64, round_iters=50, max_iter=10000, refine_every=50, tol=1e-8,
+                 criterion=CRIT_REF, parts=0, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
+        self.L = _bind_batch(load_library())
+        o = ServeOptsC()
+        self.L.e3d_serve_opts_defaults(C.byref(o))
+        o.device, o.max_active, o.round_iters, o.max_iter = device, max_active, round_iters, max_iter
+        o.refine_every, o.tol, o.criterion, o.parts = refine_every, tol, criterion, parts
+        o.e1, o.nu1, o.hbm_budget = e1, nu1, hbm_budget
+        self._h = C.c_void_p()
+        _check(self.L.e3d_serve_create(C.byref(self._h), C.byref(o)), "e3d_serve_create")
+
+    def submit(self, rve: dict, strain) -> int:
+        keep = []
+        r = _rve_struct(rve, keep)
+        s = np.ascontiguousarray(strain, dtype=np.float64)
+        rid = C.c_int64()
+        _check(self.L.e3d_serve_submit(self._h, C.byref(r), _dp(s), C.byref(rid)), "e3d_serve_submit")
+        return rid.value
+
+    def step(self) -> int:
+        pend = C.c_int32()
+        _check(self.L.e3d_serve_step(self._h, C.byref(pend)), "e3d_serve_step")
+        return pend.value
+
+    def result(self, rid: int):
+        r = JobResultC()
+        rc = self.L.e3d_serve_result(self._h, int(rid), C.byref(r))
+        if rc == E3D_ERR_STATE:
+            return None
+        _check(rc, "e3d_serve_result")
+        return r.as_dict()
+
+    def memory(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.L.e3d_serve_memory(self._h, C.byref(a), C.byref(b)), "e3d_serve_memory")
+        return a.value, b.value
+
+    def close(self):
+        if self._h:
+            self.L.e3d_serve_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

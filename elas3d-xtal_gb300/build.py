@@ -48,7 +48,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    cu_units = ["e3d_gpu", "e3d_noalloc"]
+    cu_units = ["e3d_gpu", "e3d_noalloc", "e3d_batch"]
     cu_objs = [os.path.join(OUT, u + ".o") for u in cu_units]
     cpp_obj = os.path.join(OUT, "microgen.o")
     cu_cmds = []

@@ -370,7 +370,7 @@ __global__ void apply_finish_kernel(GridDims G, const T* __restrict__ yin, const
 
 // energy_OpenMP tail (src/elas3dxtal_pcg.f90:1332-1340): g = Ku + b,
 // partial sums of (u.Ku/2 + b.u) and of g.g (gg0, :452).
-__global__ void __launch_bounds__(256) energy_finish_kernel(GridDims G, const double* __restrict__ ku,
+static __global__ void __launch_bounds__(256) energy_finish_kernel(GridDims G, const double* __restrict__ ku,
                                                             const double* __restrict__ hx,
                                                             const double* __restrict__ hy,
                                                             const double* __restrict__ hd,
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) energy_finish_kernel(GridDims G, const do
 }
 
 // Sums n partials of stride `stride` in a fixed order (single block).
-__global__ void reduce_partials_kernel(const double* __restrict__ partial, int n, int stride,
+static __global__ void reduce_partials_kernel(const double* __restrict__ partial, int n, int stride,
                                        int nfields, double* __restrict__ out) {
   __shared__ double red[8];
   for (int f = 0; f < nfields; ++f) {
@@ -424,7 +424,7 @@ struct FematParams {
 };
 
 // rotatestiffnessby (src/elas3dxtal_pcg.f90:2535-2633) for one grain.
-__device__ void bond_rotate(const double r[3], double c11, double c12, double c44, double out[6][6]) {
+static __device__ void bond_rotate(const double r[3], double c11, double c12, double c44, double out[6][6]) {
   double Cc[6][6];
   for (int i = 0; i < 6; ++i)
     for (int j = 0; j < 6; ++j) Cc[i][j] = 0.0;
@@ -494,9 +494,9 @@ __device__ void bond_rotate(const double r[3], double c11, double c12, double c4
 }
 
 // Reference local node r (1..8 -> 0..7) to corner index a = ox + 2oy + 4oz.
-__constant__ int kRefToCorner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+static __constant__ int kRefToCorner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 
-__global__ void femat_phase_kernel(FematParams P, const double* __restrict__ rod, double* __restrict__ cmod,
+static __global__ void femat_phase_kernel(FematParams P, const double* __restrict__ rod, double* __restrict__ cmod,
                                    double* __restrict__ cs, float* __restrict__ cs32,
                                    double* __restrict__ dk, double* __restrict__ dkd) {
   const int p = blockIdx.x;
@@ -583,7 +583,7 @@ __device__ __forceinline__ void element_delta(const GridDims& G, const JumpParam
   }
 }
 
-__global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+static __global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
                                const double* __restrict__ dk, double* __restrict__ b) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
@@ -618,7 +618,7 @@ __global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* __restri
 }
 
 // Constant C = 1/2 sum_e delta_e^T K_e delta_e over boundary elements.
-__global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+static __global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
                                                       const double* __restrict__ dk, double* partial) {
   __shared__ double red[8];
   double acc = 0.0;
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpParams J, 
 }
 
 // Affine initial guess (src/elas3dxtal_pcg.f90:423-438).
-__global__ void affine_kernel(GridDims G, JumpParams J, double* __restrict__ u) {
+static __global__ void affine_kernel(GridDims G, JumpParams J, double* __restrict__ u) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
   const double x = (double)(m % G.nx);
@@ -708,7 +708,7 @@ __device__ __forceinline__ void invert3x3(const double a[3][3], double ai[3][3])
 // Block-Jacobi (src/elas3dxtal_pcg.f90:1498-1520): sum of the node's diagonal
 // 3x3 blocks over its 8 elements (reference order), inverted.  Stores the
 // symmetric inverse as 6 SoA planes (00 11 22 01 02 12) in FP64 and FP32.
-__global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pix, const double* __restrict__ dkd,
+static __global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pix, const double* __restrict__ dkd,
                                double* __restrict__ minv, float* __restrict__ minv32) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
@@ -791,7 +791,7 @@ __device__ __forceinline__ void voxel_strain(const GridDims& G, const JumpParams
   eps[5] = dY[0] + dX[1];
 }
 
-__global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+static __global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
                                                          const double* __restrict__ cmod, int nphase,
                                                          const double* __restrict__ u, double* partial) {
   __shared__ double red[8];
@@ -818,7 +818,7 @@ __global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, JumpParams 
   }
 }
 
-__global__ void stress_field_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
+static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
                                     const double* __restrict__ cmod, int nphase, const double* __restrict__ u,
                                     double* __restrict__ sigma, double* __restrict__ vm) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -854,6 +854,7 @@ __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32_t* __r
 struct PcgState {
   double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
   int it, status, reset, resets, cur, max_iter, divergence_reset, refinements;
+  int since_replace, pad;
 };
 
 struct GridBarrier {
@@ -864,7 +865,7 @@ struct GridBarrier {
 // Grid-wide barrier for a cooperative launch.  Waits are bounded by a
 // wall-clock limit (globaltimer) and an iteration cap; on expiry, or when
 // another block has flagged an error, it returns false and the caller exits.
-__device__ bool grid_barrier(GridBarrier* gb, int* err, unsigned long long timeout_ns) {
+static __device__ bool grid_barrier(GridBarrier* gb, int* err, unsigned long long timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -903,7 +904,7 @@ __device__ bool grid_barrier(GridBarrier* gb, int* err, unsigned long long timeo
 }
 
 // Sum of n per-block partials in a fixed order, returned to every thread.
-__device__ double reduce_broadcast(const double* partial, int n, double* red) {
+static __device__ double reduce_broadcast(const double* partial, int n, double* red) {
   __shared__ double s_val;
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + i);
@@ -1098,7 +1099,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(GridDims G, const T* __re
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-__global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int n, double gg0_ref,
+static __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int n, double gg0_ref,
                                         int criterion, float tol, int max_iter, int divergence_reset,
                                         PcgState* st) {
   __shared__ double red[8];
@@ -1123,6 +1124,8 @@ __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int 
     S.max_iter = max_iter;
     S.divergence_reset = divergence_reset;
     S.refinements = 0;
+    S.since_replace = 0;
+    S.pad = 0;
     *st = S;
   }
 }
@@ -1130,7 +1133,7 @@ __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP64 residual replacement between FP32 inner chunks.
 // u64 += du32 ; du32 = 0 (the inner loop restarts its correction at zero).
-__global__ void fold_correction_kernel(long long n3, const float* __restrict__ du, double* __restrict__ u,
+static __global__ void fold_correction_kernel(long long n3, const float* __restrict__ du, double* __restrict__ u,
                                        float* __restrict__ du_zero) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n3) return;
@@ -1140,7 +1143,7 @@ __global__ void fold_correction_kernel(long long n3, const float* __restrict__ d
 
 // g = K u + b from the FP64 stencil (in-tile part + halos), stored in FP64 and
 // FP32; then z32 = Minv32 g32 and partial z.g for the replaced residual.
-__global__ void __launch_bounds__(256) true_residual_kernel(GridDims G, const double* __restrict__ ku,
+static __global__ void __launch_bounds__(256) true_residual_kernel(GridDims G, const double* __restrict__ ku,
                                                             const double* __restrict__ hx,
                                                             const double* __restrict__ hy,
                                                             const double* __restrict__ hd,
@@ -1180,7 +1183,7 @@ __global__ void __launch_bounds__(256) true_residual_kernel(GridDims G, const do
 // Scalars after a residual replacement: gg from the true residual, gamma
 // re-derived from it (the direction h is kept), and a convergence flag that
 // only stands if the true residual also meets the tolerance.
-__global__ void replace_scalars_kernel(const double* __restrict__ partial, int n, PcgState* st,
+static __global__ void replace_scalars_kernel(const double* __restrict__ partial, int n, PcgState* st,
                                        double* history) {
   __shared__ double red[8];
   double s = 0.0;
@@ -1206,7 +1209,7 @@ __global__ void replace_scalars_kernel(const double* __restrict__ partial, int n
 }
 
 // g32 = (float) g64 at the start of a mixed solve.
-__global__ void to_float_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
+static __global__ void to_float_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
 }

@@ -63,3 +63,29 @@ def c3(n: int = 400, ngrains: int | None = None, A: float = 2.0, seed: int = 3, 
 def random_field(ns: int, seed: int) -> np.ndarray:
     """A seeded random nodal vector (3*ns, SoA) for apply tests."""
     return np.random.default_rng(seed).standard_normal(3 * ns)
+
+
+def rve(n, ngrains, seed, A=2.0, pore_frac=0.0, shape=None):
+    """One RVE as the batch / serving APIs take it (dict)."""
+    nx, ny, nz = shape if shape is not None else (n, n, n)
+    pix, rod = micro_grains(nx, ny, nz, ngrains, seed)
+    if pore_frac > 0.0:
+        micro_spherical_pores(pix, nx, ny, nz, pore_frac, ngrains + 1, seed + 7919)
+    return dict(shape=(nx, ny, nz), ngrains=ngrains, c11=C11, c12=C12, c44=c44_from_zener(A), pix=pix,
+                rodrigues=rod)
+
+
+def ensemble(count, seed=4, edge=(32, 96), grains=(8, 200), zener=(0.5, 0.75, 1, 1.5, 2, 3, 4, 5),
+             pores=(0.0, 0.02)):
+    """The batched effective-stiffness ensemble: uneven RVE edges drawn
+    uniformly from `edge`, grain counts from `grains`, Zener ratios from
+    `zener`, pore fractions uniform in `pores`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.integers(edge[0], edge[1] + 1))
+        ng = int(rng.integers(grains[0], grains[1] + 1))
+        A = float(rng.choice(zener))
+        pf = float(rng.uniform(*pores))
+        out.append(rve(n, ng, seed * 1000 + i, A=A, pore_frac=pf))
+    return out

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared():
     names = set()
-    for h in ("e3d_gpu.h", "e3d_micro.h"):
+    for h in ("e3d_gpu.h", "e3d_micro.h", "e3d_batch.h"):
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         names |= set(re.findall(r"\b(e3d_[A-Za-z0-9_]+)\s*\(", text))

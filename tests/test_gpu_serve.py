@@ -1,0 +1,78 @@
+"""Continuous-batching server: requests admitted while others run, results
+against the FP64 oracle, the same result alone and in the mix, admission
+bounded by the HBM budget."""
+import numpy as np
+import pytest
+
+import elas3d_xtal_gb300 as e3d
+import oracle as O
+from elas3d_xtal_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+ENERGY_TOL = 1e-8
+
+
+def _oracle(rve, strain):
+    nx, ny, nz = rve["shape"]
+    s = strain
+    p = O.Problem(nx, ny, nz, rve["ngrains"] + 1, c11=rve["c11"], c12=rve["c12"], c44=rve["c44"],
+                  exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5])
+    return O.run(p, rve["pix"], rve["rodrigues"])
+
+
+def _requests():
+    rng = np.random.default_rng(7)
+    reqs = []
+    for i, n in enumerate([14, 22, 10, 18, 26]):
+        rve = W.rve(n, int(rng.integers(4, 12)), 100 + i, A=float(rng.uniform(0.5, 5.0)),
+                    pore_frac=float(rng.uniform(0, 0.03)))
+        strain = rng.normal(size=6) * 1e-3
+        reqs.append((rve, strain))
+    return reqs
+
+
+def _drain(srv, ids, rounds=100000):
+    for _ in range(rounds):
+        if srv.step() == 0:
+            break
+    return [srv.result(i) for i in ids]
+
+
+def test_serve_results_match_oracle_and_mix():
+    reqs = _requests()
+    # alone: request 1 in a fresh server
+    with e3d.Server(round_iters=10) as srv:
+        rid = srv.submit(*reqs[1])
+        alone = _drain(srv, [rid])[0]
+    # mixed: staggered arrivals while others are on the device
+    with e3d.Server(round_iters=10) as srv:
+        ids = [srv.submit(*reqs[0]), srv.submit(*reqs[1])]
+        srv.step()
+        srv.step()
+        ids += [srv.submit(*r) for r in reqs[2:]]
+        out = _drain(srv, ids)
+    for (rve, strain), r in zip(reqs, out):
+        assert r is not None and r["status"] == e3d.EXIT_CONVERGED, r
+        ref = _oracle(rve, strain)
+        assert abs(r["utot"] - ref["utot"]) <= ENERGY_TOL * abs(ref["utot"])
+        assert r["seconds"] > 0
+    mixed = out[1]
+    assert mixed["iterations"] == alone["iterations"]
+    assert abs(mixed["utot"] - alone["utot"]) <= 1e-12 * abs(alone["utot"])
+    assert np.array_equal(mixed["strav"], alone["strav"])
+
+
+def test_serve_hbm_budget_bounds_admission():
+    reqs = _requests()
+    with e3d.Server(round_iters=20) as probe:
+        probe.submit(*reqs[4])
+        probe.step()
+        one, _ = probe.memory()
+    budget = int(one * 1.5)  # room for the largest request alone
+    with e3d.Server(round_iters=20, hbm_budget=budget) as srv:
+        ids = [srv.submit(*r) for r in reqs]
+        out = _drain(srv, ids)
+        now, peak = srv.memory()
+    assert all(r is not None and r["status"] == e3d.EXIT_CONVERGED for r in out)
+    assert peak <= budget and now == 0
