@@ -355,6 +355,173 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The three added forms (the benchmark spec): full solves FP64 vs mixed, the batched
+# effective-stiffness ensemble and the continuous-batching server.  Each prints
+# its own JSON line; the default run prints the plain-FP64 line above.
+def _full_solve(e3d, p, pix, rod, precision):
+    p.precision = precision
+    p.max_iter = 100000
+    g = e3d.Elas3D(p)
+    g.upload(pix, rod)
+    t0 = time.perf_counter()
+    r = g.run()
+    dt = time.perf_counter() - t0
+    g.close()
+    r["seconds"] = dt
+    return r
+
+
+def run_form_solve(args):
+    e3d = _load_package()
+    p, pix, rod = _workload(args.n)
+    p.criterion = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
+    a = _full_solve(e3d, p, pix, rod, e3d.PREC_FP64)
+    b = _full_solve(e3d, p, pix, rod, e3d.PREC_MIXED)
+    err = abs(b["utot"] - a["utot"]) / abs(a["utot"])
+    serr = float(((b["strav"] - a["strav"]) ** 2).sum() ** 0.5 / (a["strav"] ** 2).sum() ** 0.5)
+    line = {"metric": f"time to solution, {args.n}^3 (s)", "form": "solve", "unit": "s", "higher_is_better": False,
+            "value": b["seconds"], "fp64_seconds": a["seconds"], "speedup_mixed_vs_fp64": a["seconds"] / b["seconds"],
+            "iterations": {"fp64": a["iterations"], "mixed": b["iterations"]}, "refinements": b["refinements"],
+            "energy_rel_err_mixed_vs_fp64": err, "stress_rel_err_mixed_vs_fp64": serr,
+            "criterion": args.criterion, "true_rel": {"fp64": a["true_rel"], "mixed": b["true_rel"]},
+            "config": {"workload": f"c2_polycrystal_{args.n}", "dof": 3 * p.ns, "includes": "femat, energy x2, PCG, stress"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_form_batch(args):
+    import numpy as np
+
+    e3d = _load_package()
+    from elas3d_xtal_gb300 import workloads as W
+
+    rves = W.ensemble(args.rves, seed=4)
+    nodes = sum(int(np.prod(r["shape"])) for r in rves)
+    t0 = time.perf_counter()
+    crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
+    b = e3d.Batch(rves, max_iter=20000, criterion=crit)
+    t_create = time.perf_counter() - t0
+    ceff, sec = b.solve()  # first solve
+    ceff, sec = b.solve()  # graph replay (timed)
+    res = b.results()
+    parts = b.parts()
+    b.close()
+    nj = len(res)
+    iters = [r["iterations"] for r in res]
+    conv = sum(r["status"] == e3d.EXIT_CONVERGED for r in res)
+    # reference: plain sequential FP64 GPU solves of a seeded sample of the same jobs
+    rng = np.random.default_rng(0)
+    sample = rng.choice(nj, size=min(args.sample, nj), replace=False)
+    seq, errs = [], []
+    for j in sample:
+        r = res[int(j)]
+        rv = rves[r["rve"]]
+        s = [0.0] * 6
+        s[r["load_case"]] = 1e-3 if r["load_case"] < 3 else 0.5e-3
+        p = e3d.Problem(*rv["shape"], rv["ngrains"] + 1, c11=rv["c11"], c12=rv["c12"], c44=rv["c44"], strain=tuple(s))
+        p.criterion = crit
+        rr = _full_solve(e3d, p, rv["pix"], rv["rodrigues"], e3d.PREC_FP64)
+        seq.append(rr["seconds"])
+        errs.append(abs(rr["utot"] - r["utot"]) / abs(rr["utot"]))
+    seq_rate = len(seq) / sum(seq)
+    line = {"metric": "batched solves/s (256 RVEs x 6 load cases, mixed precision)", "form": "batch",
+            "value": nj / sec, "unit": "solves/s", "higher_is_better": True, "seconds": sec,
+            "solves": nj, "converged": conv, "iterations": {"min": min(iters), "max": max(iters),
+                                                           "mean": float(np.mean(iters))},
+            "parts_hist": {str(k): int((parts == k).sum()) for k in sorted(set(parts.tolist()))},
+            "create_seconds": t_create, "rve_nodes": nodes,
+            "sequential_fp64": {"solves_per_s": seq_rate, "sample": len(seq),
+                                "sample_seconds": sum(seq),
+                                "energy_rel_err_vs_batched": {"max": max(errs), "median": float(np.median(errs))}},
+            "criterion": args.criterion,
+            "speedup_vs_sequential_fp64": (nj / sec) / seq_rate,
+            "config": {"workload": "ensemble", "rves": len(rves), "edges": "U{32..96}", "grains": "8-200",
+                       "zener": "{0.5,0.75,1,1.5,2,3,4,5}", "pores": "0-2 %", "load_cases": 6,
+                       "launch": "one persistent launch from a CUDA graph"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_form_serve(args):
+    import numpy as np
+
+    e3d = _load_package()
+    from elas3d_xtal_gb300 import workloads as W
+
+    rng = np.random.default_rng(5)
+    reqs = []
+    for i in range(args.requests):
+        n = int(rng.integers(48, args.serve_max_edge + 1))
+        ng = int(rng.integers(16, 1001))
+        A = float(rng.uniform(0.5, 5.0))
+        pf = float(rng.uniform(0.0, 0.03))
+        rv = W.rve(n, ng, 5000 + i, A=A, pore_frac=pf)
+        lc = int(rng.integers(0, 6))
+        s = np.zeros(6)
+        s[lc] = 1e-3 if lc < 3 else 0.5e-3
+        reqs.append((rv, s))
+    gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
+    arrivals = np.cumsum(gaps)
+    budget = int(150e9)
+    crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
+    srv = e3d.Server(max_active=args.slots, round_iters=args.round_iters, max_iter=20000, hbm_budget=budget,
+                     criterion=crit)
+    t0 = time.perf_counter()
+    ids, done_at = [], {}
+    i = 0
+    while True:
+        now = time.perf_counter() - t0
+        while i < len(reqs) and arrivals[i] <= now:
+            ids.append(srv.submit(*reqs[i]))
+            i += 1
+        pend = srv.step()
+        now = time.perf_counter() - t0
+        for k, rid in enumerate(ids):
+            if rid not in done_at and srv.result(rid) is not None:
+                done_at[rid] = now
+        if i >= len(reqs) and pend == 0:
+            break
+        if pend == 0 and i < len(reqs):
+            time.sleep(max(0.0, arrivals[i] - now))
+    total = time.perf_counter() - t0
+    res = [srv.result(r) for r in ids]
+    _, peak = srv.memory()
+    srv.close()
+    lat = np.array([done_at[rid] - arrivals[k] for k, rid in enumerate(ids)])
+    conv = sum(r["status"] == e3d.EXIT_CONVERGED for r in res)
+    # reference: the same requests as plain sequential FP64 GPU solves (sample)
+    m = min(args.sample, len(reqs))
+    seq, errs = [], []
+    for (rv, s), r in list(zip(reqs, res))[:m]:
+        p = e3d.Problem(*rv["shape"], rv["ngrains"] + 1, c11=rv["c11"], c12=rv["c12"], c44=rv["c44"], strain=tuple(s))
+        p.criterion = crit
+        rr = _full_solve(e3d, p, rv["pix"], rv["rodrigues"], e3d.PREC_FP64)
+        seq.append(rr["seconds"])
+        errs.append(abs(rr["utot"] - r["utot"]) / abs(rr["utot"]))
+    # sequential service of the sampled arrivals: latency = finish - arrival
+    tq, seq_lat = 0.0, []
+    for a, d in zip(arrivals[:m], seq):
+        tq = max(tq, a) + d
+        seq_lat.append(tq - a)
+    line = {"metric": "served solves/s (Poisson 200/s, edges 48-256, mixed precision)", "form": "serve",
+            "value": len(reqs) / total, "unit": "solves/s", "higher_is_better": True, "requests": len(reqs),
+            "converged": conv, "wall_seconds": total, "latency_s": {"p50": float(np.percentile(lat, 50)),
+                                                                   "p99": float(np.percentile(lat, 99)),
+                                                                   "max": float(lat.max())},
+            "peak_hbm_bytes": peak, "hbm_budget": budget, "slots": args.slots, "round_iters": args.round_iters,
+            "criterion": args.criterion,
+            "sequential_fp64": {"sample": m, "solves_per_s": m / sum(seq),
+                                "energy_rel_err_vs_served": {"max": max(errs), "median": float(np.median(errs))},
+                                "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
+                                              "p99": float(np.percentile(seq_lat, 99))}},
+            "config": {"workload": "serve", "arrivals": f"Poisson, mean {args.rate}/s, seed 5",
+                       "edges": f"U{{48..{args.serve_max_edge}}}", "grains": "16-1000", "zener": "U[0.5,5]",
+                       "pores": "0-3 %", "load": "one unit load case per request"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,11 +531,28 @@ def main():
     ap.add_argument("--n", type=int, default=500, help="grid edge (default: the 500^3 config)")
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--form", choices=["plain", "solve", "batch", "serve"], default="plain",
+                    help="plain: the FP64 DOF-iters/s line; solve/batch/serve: the added forms")
+    ap.add_argument("--rves", type=int, default=256, help="batch: ensemble size")
+    ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=64, help="serve: concurrent solves")
+    ap.add_argument("--round-iters", type=int, default=50, help="serve: iterations per solve per round")
+    ap.add_argument("--serve-max-edge", type=int, default=256)
+    ap.add_argument("--sample", type=int, default=16, help="batch/serve: sequential FP64 reference sample")
+    ap.add_argument("--criterion", choices=["ref", "precond"], default="ref",
+                    help="forms: ref = sqrt(z.g/|g0|^2) (the reference's test), precond = sqrt(z.g/z0.g0)")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         ap.error("steps >= 1 and warmup >= 0")
     if args.impl == "reference":
         return run_reference(args)
+    if args.form == "solve":
+        return run_form_solve(args)
+    if args.form == "batch":
+        return run_form_batch(args)
+    if args.form == "serve":
+        return run_form_serve(args)
     return run_ours(args)
 
 
