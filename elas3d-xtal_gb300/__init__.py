@@ -42,6 +42,7 @@ E3D_ERR_STATE = 7
 
 EXIT_CONVERGED, EXIT_HAH_GUARD, EXIT_MAXITER, EXIT_BREAKDOWN, EXIT_TIMEOUT, EXIT_RUNNING = range(6)
 CRIT_REF, CRIT_PRECOND_REL = 0, 1
+PRECOND_BLOCK_JACOBI, PRECOND_NONE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 
 # Every symbol include/e3d_gpu.h and include/e3d_micro.h declare.
@@ -52,7 +53,8 @@ EXPORTED_SYMBOLS = (
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
     "e3d_device_bytes", "e3d_launch_count", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
-    "e3d_apply_noalloc",
+    "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
+    "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
     "e3d_euler_to_rodrigues",
 )
@@ -73,6 +75,7 @@ class ProblemC(C.Structure):
         ("flag_m", C.c_int32), ("criterion", C.c_int32), ("precision", C.c_int32),
         ("divergence_reset", C.c_int32), ("max_iter", C.c_int32), ("device", C.c_int32),
         ("tol", C.c_float), ("refine_every", C.c_int32),
+        ("preconditioner", C.c_int32), ("reserved", C.c_int32),
         ("c11", C.c_double), ("c12", C.c_double), ("c44", C.c_double),
         ("e1", C.c_double), ("nu1", C.c_double), ("strain", C.c_double * 6),
         ("hbm_budget", C.c_int64),
@@ -130,6 +133,11 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_launch_count.restype = C.c_int64
     L.e3d_probe_peaks.argtypes = [C.c_int32, dp, dp]
     L.e3d_apply_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp]
+    L.e3d_checkpoint_save.argtypes = [vp, C.c_char_p]
+    L.e3d_checkpoint_load.argtypes = [vp, C.c_char_p]
+    L.e3d_micro_write.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, dp]
+    L.e3d_micro_read_header.argtypes = [C.c_char_p, ip, ip, ip, ip]
+    L.e3d_micro_read.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, dp]
     L.e3d_strerror.argtypes = [C.c_int32]
     L.e3d_strerror.restype = C.c_char_p
     L.e3d_last_cuda_error.argtypes = []
@@ -200,6 +208,7 @@ class Problem:
     precision: int = PREC_FP64
     divergence_reset: int = 1
     refine_every: int = 0
+    preconditioner: int = PRECOND_BLOCK_JACOBI
     device: int = 0
     hbm_budget: int = 0
 
@@ -213,6 +222,7 @@ class Problem:
         p.flag_m, p.criterion, p.precision = self.flag_m, self.criterion, self.precision
         p.divergence_reset, p.max_iter, p.device = self.divergence_reset, self.max_iter, self.device
         p.tol, p.refine_every = self.tol, self.refine_every
+        p.preconditioner, p.reserved = self.preconditioner, 0
         p.c11, p.c12, p.c44, p.e1, p.nu1 = self.c11, self.c12, self.c44, self.e1, self.nu1
         for i in range(6):
             p.strain[i] = float(self.strain[i])
@@ -374,6 +384,12 @@ class Elas3D:
         _check(self.L.e3d_get_history(self._h, _dp(out), n, C.byref(cnt)), "e3d_get_history")
         return out[: cnt.value].copy()
 
+    def checkpoint_save(self, path: str):
+        _check(self.L.e3d_checkpoint_save(self._h, os.fsencode(path)), "e3d_checkpoint_save")
+
+    def checkpoint_load(self, path: str):
+        _check(self.L.e3d_checkpoint_load(self._h, os.fsencode(path)), "e3d_checkpoint_load")
+
     def device_bytes(self) -> int:
         return int(self.L.e3d_device_bytes(self._h))
 
@@ -428,6 +444,33 @@ def probe_peaks(device: int = 0):
     a, b = C.c_double(), C.c_double()
     _check(load_library().e3d_probe_peaks(device, C.byref(a), C.byref(b)), "e3d_probe_peaks")
     return a.value, b.value
+
+
+def micro_write(path, pix, rod, shape):
+    """Writes the .e3d container (pix 1-based, rod 3*ngrains)."""
+    pix = np.ascontiguousarray(pix, dtype=np.int32).reshape(-1)
+    rod = np.ascontiguousarray(rod, dtype=np.float64).reshape(-1)
+    nx, ny, nz = shape
+    rc = load_library().e3d_micro_write(os.fsencode(path), nx, ny, nz, rod.size // 3, _ip(pix), _dp(rod))
+    if rc != 0:
+        raise OSError(f"e3d_micro_write({path}) failed ({rc})")
+
+
+def micro_read(path):
+    """Reads a .e3d container: returns (pix, rod, (nx, ny, nz)); raises on the
+    reference's size / phase-range checks."""
+    L = load_library()
+    d = [C.c_int32() for _ in range(4)]
+    rc = L.e3d_micro_read_header(os.fsencode(path), *[C.byref(v) for v in d])
+    if rc != 0:
+        raise OSError(f"{path}: not a .e3d file ({rc})")
+    nx, ny, nz, ng = (v.value for v in d)
+    pix = np.empty(nx * ny * nz, np.int32)
+    rod = np.empty(3 * ng)
+    rc = L.e3d_micro_read(os.fsencode(path), nx, ny, nz, ng, _ip(pix), _dp(rod))
+    if rc != 0:
+        raise ValueError(f"{path}: size or phase-range check failed ({rc})")
+    return pix, rod, (nx, ny, nz)
 
 
 def euler_to_rodrigues(euler: np.ndarray) -> np.ndarray:

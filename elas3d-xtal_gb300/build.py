@@ -20,6 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libe3d_gpu.so")
+DRIVER = os.path.join(OUT, "e3d_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -31,15 +32,17 @@ def _nvcc() -> str:
 
 
 def _sources():
+    drv = os.path.join(PKG, "driver")
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
             if f.endswith((".cu", ".cuh", ".cpp", ".h"))] + \
-           [os.path.join(INCLUDE, f) for f in sorted(os.listdir(INCLUDE)) if f.endswith(".h")]
+           [os.path.join(INCLUDE, f) for f in sorted(os.listdir(INCLUDE)) if f.endswith(".h")] + \
+           [os.path.join(drv, f) for f in sorted(os.listdir(drv)) if f.endswith(".cpp")]
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(DRIVER):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(DRIVER))
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
@@ -72,6 +75,11 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     link = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *cu_objs, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
     logs.append(run(link))
     os.replace(LIB + ".tmp", LIB)
+    # command-line driver (mirrors `program elas3d`), linked against the library
+    drv = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, os.path.join(PKG, "driver", "e3d_run.cpp"),
+           "-L", OUT, "-le3d_gpu", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    logs.append(run(drv))
+    os.replace(DRIVER + ".tmp", DRIVER)
     if verbose or ptxas_info:
         sys.stdout.write("".join(logs))
     return LIB

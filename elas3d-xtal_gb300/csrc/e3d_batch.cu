@@ -32,7 +32,8 @@ namespace {
     }                                                \
   } while (0)
 
-constexpr int kPartChoices[] = {1, 2, 4, 8, 16};
+constexpr int kPartChoices[] = {1, 2, 4, 8, 16, 32, 64};
+constexpr int kMaxParts = 64;
 constexpr unsigned long long kTimeoutNs = 120ull * 1000000000ull;
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -62,7 +63,7 @@ long long halo_doubles(const GridDims& G) { return 3LL * G.ntiles * G.tz * (TILE
 
 long long max_halo_doubles(int nx, int ny, int nz) {
   long long m = 0;
-  for (int k = 1; k <= 16; ++k) m = std::max(m, halo_doubles(job_dims(nx, ny, nz, k)));
+  for (int k = 1; k <= kMaxParts; ++k) m = std::max(m, halo_doubles(job_dims(nx, ny, nz, k)));
   return m;
 }
 
@@ -121,7 +122,7 @@ size_t rve_bytes(long long ns, int nphase) {
 size_t job_bytes(int nx, int ny, int nz) {
   const long long ns = (long long)nx * ny * nz, n3 = 3 * ns;
   return 3 * align256(8 * n3) + 6 * align256(4 * n3) + align256(8 * max_halo_doubles(nx, ny, nz)) +
-         align256(8 * kJobSlots * 16) + align256(sizeof(GridBarrier)) + align256(sizeof(PcgState)) + align256(4) +
+         align256(8 * kJobSlots * kMaxParts) + align256(sizeof(GridBarrier)) + align256(sizeof(PcgState)) + align256(4) +
          align256(sizeof(JobResult));
 }
 
@@ -203,7 +204,7 @@ void fill_job(JobDev& J, const RveDev& R, char*& p, const double strain[6], int 
   J.halo_cap = max_halo_doubles(R.nx, R.ny, R.nz);
   double* halo = carve<double>(p, (size_t)J.halo_cap);
   d.hx = halo;  // split per k in set_parts
-  d.partial = carve<double>(p, (size_t)kJobSlots * 16);
+  d.partial = carve<double>(p, (size_t)kJobSlots * kMaxParts);
   d.bar = carve<GridBarrier>(p, 1);
   d.st = carve<PcgState>(p, 1);
   d.stage = carve<int>(p, 1);
@@ -226,9 +227,9 @@ void set_parts(JobDev& J, const RveDev& R, int k) {
 }
 
 int default_parts(long long ns) {
-  // about 128K nodes per block, at most 16 blocks per solve
+  // about 128K nodes per block, at most kMaxParts blocks per solve
   int k = 1;
-  while (k < 16 && ns > (long long)k * 131072) k *= 2;
+  while (k < kMaxParts && ns > (long long)k * 131072) k *= 2;
   return k;
 }
 
@@ -518,7 +519,7 @@ int32_t e3d_batch_create(e3d_batch_t** out, const e3d_rve_t* rves, int32_t n, co
   // blocks per solve
   std::vector<int> kjob(b->jobs.size(), 1);
   if (o->parts > 0) {
-    for (size_t j = 0; j < b->jobs.size(); ++j) kjob[j] = std::min(o->parts, 16);
+    for (size_t j = 0; j < b->jobs.size(); ++j) kjob[j] = std::min(o->parts, kMaxParts);
   } else if ((rc = batch_autotune(b, kjob))) {
     return fail(rc);
   }
@@ -757,12 +758,16 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
     }
     fill_job(j->J, j->R, p, j->strain, s->opts.max_iter, s->opts.refine_every, s->opts.criterion,
              s->opts.divergence_reset, s->opts.tol);
-    const int k = s->opts.parts > 0 ? std::min(s->opts.parts, 16) : default_parts(ns);
+    const int k = s->opts.parts > 0 ? std::min(s->opts.parts, kMaxParts) : default_parts(ns);
     set_parts(j->J, j->R, std::min(k, s->eng.grid));
     BCUDA(cudaMemsetAsync(j->J.d.stage, 0, 4, s->stream));
     s->active.push_back(j);
   }
   if (!s->active.empty()) {
+    // largest solves first: their parts start early and the round's tail is
+    // filled with small ones
+    std::stable_sort(s->active.begin(), s->active.end(),
+                     [](const ServeJob* a, const ServeJob* c) { return a->R.ns > c->R.ns; });
     std::vector<JobDesc> descs;
     for (ServeJob* j : s->active) descs.push_back(j->J.d);
     int np = 0;

@@ -253,6 +253,7 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
   if ((long long)p->nx * p->ny * p->nz > (1LL << 40)) return E3D_ERR_INPUT;
   if (p->precision != E3D_PREC_FP64 && p->precision != E3D_PREC_MIXED) return E3D_ERR_INPUT;
   if (p->criterion != E3D_CRIT_REF && p->criterion != E3D_CRIT_PRECOND_REL) return E3D_ERR_INPUT;
+  if (p->preconditioner != E3D_PRECOND_BLOCK_JACOBI && p->preconditioner != E3D_PRECOND_NONE) return E3D_ERR_INPUT;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
@@ -445,8 +446,8 @@ int32_t e3d_solve_begin(e3d_handle_t* h) {
   E3D_CUDA(cudaEventRecord(e0, h->stream));
   // block-Jacobi (kkk == 1, src/elas3dxtal_pcg.f90:1498-1520); the mixed form
   // keeps an FP32 copy of the FP64 inverse.
-  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->pix, h->dkd, h->minv,
-                                                                   mixed ? h->minv32 : nullptr);
+  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(
+      h->G, h->pix, h->dkd, h->minv, mixed ? h->minv32 : nullptr, h->prob.preconditioner == E3D_PRECOND_NONE);
   E3D_LAUNCHED(h);
   const int grid = reduction_grid(h);
   if (mixed) {
@@ -901,4 +902,129 @@ extern "C" int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* 
   int32_t rc = run_probe<double>(device, fp64_tflops);
   if (rc) return rc;
   return run_probe<float>(device, fp32_tflops);
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint / resume.  File: 16-byte header "E3DCKPT1" + version, the problem
+// dimensions and forms, gg0, the PcgState, then the state arrays and the
+// rel_res history (host byte order).
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz, nphase, precision, criterion, preconditioner;
+  double gg0;
+  PcgState st;
+};
+
+template <typename T>
+int32_t ckpt_write(FILE* f, const T* dev, size_t count, cudaStream_t s) {
+  std::vector<T> buf(count);
+  E3D_CUDA(cudaMemcpyAsync(buf.data(), dev, sizeof(T) * count, cudaMemcpyDeviceToHost, s));
+  E3D_CUDA(cudaStreamSynchronize(s));
+  if (std::fwrite(buf.data(), sizeof(T), count, f) != count) return E3D_ERR_INPUT;
+  return E3D_OK;
+}
+
+template <typename T>
+int32_t ckpt_read(FILE* f, T* dev, size_t count, cudaStream_t s) {
+  std::vector<T> buf(count);
+  if (std::fread(buf.data(), sizeof(T), count, f) != count) return E3D_ERR_INPUT;
+  E3D_CUDA(cudaMemcpyAsync(dev, buf.data(), sizeof(T) * count, cudaMemcpyHostToDevice, s));
+  E3D_CUDA(cudaStreamSynchronize(s));
+  return E3D_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t e3d_checkpoint_save(e3d_handle_t* h, const char* path) {
+  if (!h || !path) return E3D_ERR_INPUT;
+  if (!h->solve_ready) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  const bool mixed = h->prob.precision == E3D_PREC_MIXED;
+  if (mixed) {  // u holds the current iterate, du is zero
+    int32_t rc = fold_correction(h);
+    if (rc) return rc;
+  }
+  CkptHeader H{};
+  std::memcpy(H.magic, "E3DCKPT1", 8);
+  H.version = 1;
+  H.nx = h->prob.nx;
+  H.ny = h->prob.ny;
+  H.nz = h->prob.nz;
+  H.nphase = h->prob.nphase;
+  H.precision = h->prob.precision;
+  H.criterion = h->prob.criterion;
+  H.preconditioner = h->prob.preconditioner;
+  H.gg0 = h->gg0;
+  E3D_CUDA(cudaMemcpyAsync(&H.st, h->st, sizeof(PcgState), cudaMemcpyDeviceToHost, h->stream));
+  E3D_CUDA(cudaStreamSynchronize(h->stream));
+  H.st.since_replace = h->since_replace;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return E3D_ERR_INPUT;
+  const size_t n3 = 3 * (size_t)h->G.ns;
+  int32_t rc = std::fwrite(&H, sizeof H, 1, f) == 1 ? E3D_OK : E3D_ERR_INPUT;
+  if (!rc) rc = ckpt_write(f, h->u, n3, h->stream);
+  if (!rc) rc = ckpt_write(f, h->g, n3, h->stream);
+  if (!mixed) {
+    if (!rc) rc = ckpt_write(f, h->z, n3, h->stream);
+    if (!rc) rc = ckpt_write(f, H.st.cur ? h->h1 : h->h0, n3, h->stream);
+  } else {
+    if (!rc) rc = ckpt_write(f, h->g32, n3, h->stream);
+    if (!rc) rc = ckpt_write(f, h->z32, n3, h->stream);
+    if (!rc) rc = ckpt_write(f, H.st.cur ? h->h32b : h->h32a, n3, h->stream);
+  }
+  if (!rc && H.st.it > 0) rc = ckpt_write(f, h->history, (size_t)H.st.it, h->stream);
+  if (std::fclose(f) != 0 && !rc) rc = E3D_ERR_INPUT;
+  return rc;
+}
+
+extern "C" int32_t e3d_checkpoint_load(e3d_handle_t* h, const char* path) {
+  if (!h || !path) return E3D_ERR_INPUT;
+  if (!h->femat_done) return E3D_ERR_STATE;
+  cudaSetDevice(h->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return E3D_ERR_INPUT;
+  CkptHeader H{};
+  if (std::fread(&H, sizeof H, 1, f) != 1 || std::memcmp(H.magic, "E3DCKPT1", 8) != 0 || H.version != 1 ||
+      H.nx != h->prob.nx || H.ny != h->prob.ny || H.nz != h->prob.nz || H.nphase != h->prob.nphase ||
+      H.precision != h->prob.precision || H.criterion != h->prob.criterion ||
+      H.preconditioner != h->prob.preconditioner || H.st.it > h->prob.max_iter) {
+    std::fclose(f);
+    return E3D_ERR_INPUT;
+  }
+  const bool mixed = h->prob.precision == E3D_PREC_MIXED;
+  // preconditioner of this problem (deterministic, so it is rebuilt, not stored)
+  bjacobi_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(
+      h->G, h->pix, h->dkd, h->minv, mixed ? h->minv32 : nullptr, h->prob.preconditioner == E3D_PRECOND_NONE);
+  E3D_LAUNCHED(h);
+  const size_t n3 = 3 * (size_t)h->G.ns;
+  PcgState S = H.st;
+  int32_t rc = ckpt_read(f, h->u, n3, h->stream);
+  if (!rc) rc = ckpt_read(f, h->g, n3, h->stream);
+  if (!mixed) {
+    if (!rc) rc = ckpt_read(f, h->z, n3, h->stream);
+    if (!rc) rc = ckpt_read(f, S.cur ? h->h1 : h->h0, n3, h->stream);
+  } else {
+    if (!rc) rc = ckpt_read(f, h->g32, n3, h->stream);
+    if (!rc) rc = ckpt_read(f, h->z32, n3, h->stream);
+    if (!rc) rc = ckpt_read(f, S.cur ? h->h32b : h->h32a, n3, h->stream);
+    if (!rc) {
+      E3D_CUDA(cudaMemsetAsync(h->du32, 0, sizeof(float) * n3, h->stream));
+    }
+  }
+  if (!rc && S.it > 0) rc = ckpt_read(f, h->history, (size_t)S.it, h->stream);
+  std::fclose(f);
+  if (rc) return rc;
+  E3D_CUDA(cudaMemcpyAsync(h->st, &S, sizeof S, cudaMemcpyHostToDevice, h->stream));
+  rc = sync(h);
+  if (rc) return rc;
+  h->gg0 = H.gg0;
+  h->since_replace = S.since_replace;
+  h->energy_done = true;
+  h->minv_ready = true;
+  h->solve_ready = true;
+  h->ms_setup = 0.0;
+  h->ms_iter = 0.0;
+  return E3D_OK;
 }

@@ -58,7 +58,7 @@ struct JobDesc {
   double* hx;
   double* hy;
   double* hd;
-  double* partial;  // [16][nparts]
+  double* partial;  // [kJobSlots][nparts]
   GridBarrier* bar;
   PcgState* st;
   int* stage;
@@ -149,8 +149,10 @@ __device__ __forceinline__ void for_part_nodes(const JobDesc& J, int part, F&& f
   }
 }
 
+// The heavy steps below are kept out of line so each gets its own register
+// allocation instead of the engine kernel's peak.
 template <typename T, bool FUSED>
-__device__ void job_apply(const JobDesc& J, int part, ApplyArgs<T>& A, ApplySmem<T>& sm, double& hAh) {
+__device__ __noinline__ void job_apply(const JobDesc& J, int part, ApplyArgs<T>& A, ApplySmem<T>& sm, double& hAh) {
   for (long long t = part; t < J.G.ntiles; t += J.nparts) {
     apply_tile<T, FUSED>(A, t, sm, hAh);
     __syncthreads();
@@ -158,7 +160,7 @@ __device__ void job_apply(const JobDesc& J, int part, ApplyArgs<T>& A, ApplySmem
 }
 
 // b at node m: sum over its boundary elements of the row of K_e delta_e.
-static __device__ void job_b_node(const JobDesc& J, int x, int y, int z, double (&acc)[3]) {
+static __device__ __noinline__ void job_b_node(const JobDesc& J, int x, int y, int z, double (&acc)[3]) {
   const GridDims& G = J.G;
   acc[0] = acc[1] = acc[2] = 0.0;
   if (!(x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1)) return;
@@ -181,7 +183,7 @@ static __device__ void job_b_node(const JobDesc& J, int x, int y, int z, double 
   }
 }
 
-static __device__ double job_c_elem(const JobDesc& J, int x, int y, int z) {
+static __device__ __noinline__ double job_c_elem(const JobDesc& J, int x, int y, int z) {
   const GridDims& G = J.G;
   if (!(x == G.nx - 1 || y == G.ny - 1 || z == G.nz - 1)) return 0.0;
   double d[8][3];
@@ -242,7 +244,7 @@ static __device__ bool job_fp64_apply_u(const JobDesc& J, int part, ApplySmem<do
 
 // After job_fp64_apply_u: g = Ku + b (+ halos), g32, z32 = Minv32 g32, partial z.g;
 // optionally the energy terms.  Ends with a barrier.
-static __device__ bool job_true_residual(const JobDesc& J, int part, bool energy, double* red, int* err,
+static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part, bool energy, double* red, int* err,
                                   unsigned long long to) {
   const GridDims& G = J.G;
   const long long ns = G.ns;
@@ -286,7 +288,10 @@ static __device__ void job_fold(const JobDesc& J, int part) {
   });
 }
 
-static __global__ void __launch_bounds__(NT, E3D_F32_BLOCKS_PER_SM) job_engine_kernel(EngineArgs E) {
+#ifndef E3D_ENGINE_BLOCKS_PER_SM
+#define E3D_ENGINE_BLOCKS_PER_SM 2  // resident engine blocks per SM (register budget)
+#endif
+static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engine_kernel(EngineArgs E) {
   __shared__ __align__(16) unsigned char smraw[sizeof(ApplySmem<double>)];
   __shared__ double red[NT / 32];
   __shared__ int s_idx;

@@ -709,9 +709,17 @@ __device__ __forceinline__ void invert3x3(const double a[3][3], double ai[3][3])
 // 3x3 blocks over its 8 elements (reference order), inverted.  Stores the
 // symmetric inverse as 6 SoA planes (00 11 22 01 02 12) in FP64 and FP32.
 static __global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pix, const double* __restrict__ dkd,
-                               double* __restrict__ minv, float* __restrict__ minv32) {
+                               double* __restrict__ minv, float* __restrict__ minv32, int identity = 0) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
+  if (identity) {  // plain CG: z = g
+    for (int q = 0; q < 6; ++q) {
+      const double v = q < 3 ? 1.0 : 0.0;
+      if (minv) minv[m + q * G.ns] = v;
+      if (minv32) minv32[m + q * G.ns] = (float)v;
+    }
+    return;
+  }
   const int x = (int)(m % G.nx);
   const int y = (int)((m / G.nx) % G.ny);
   const int z = (int)(m / ((long long)G.nx * G.ny));

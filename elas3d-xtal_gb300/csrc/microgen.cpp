@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -351,4 +352,71 @@ extern "C" void e3d_euler_to_rodrigues(int32_t n, const double* euler, double* r
     rod[3 * i + 1] = q2 / d;
     rod[3 * i + 2] = q3 / d;
   }
+}
+
+// ---------------------------------------------------------------------------
+// .e3d container (see include/e3d_micro.h).
+namespace {
+struct MicroHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz, ngrains, reserved;
+};
+}  // namespace
+
+extern "C" int32_t e3d_micro_write(const char* path, int32_t nx, int32_t ny, int32_t nz, int32_t ngrains,
+                                   const int32_t* pix, const double* rod) {
+  if (!path || !pix || !rod || nx < 1 || ny < 1 || nz < 1 || ngrains < 1) return -2;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return -1;
+  MicroHeader H{};
+  std::memcpy(H.magic, "E3DMICRO", 8);
+  H.version = 1;
+  H.nx = nx;
+  H.ny = ny;
+  H.nz = nz;
+  H.ngrains = ngrains;
+  const size_t ns = (size_t)nx * ny * nz;
+  bool ok = std::fwrite(&H, sizeof H, 1, f) == 1 && std::fwrite(pix, sizeof(int32_t), ns, f) == ns &&
+            std::fwrite(rod, sizeof(double), 3 * (size_t)ngrains, f) == 3 * (size_t)ngrains;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? 0 : -1;
+}
+
+extern "C" int32_t e3d_micro_read_header(const char* path, int32_t* nx, int32_t* ny, int32_t* nz,
+                                         int32_t* ngrains) {
+  if (!path) return -2;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return -1;
+  MicroHeader H{};
+  const bool ok = std::fread(&H, sizeof H, 1, f) == 1;
+  std::fclose(f);
+  if (!ok || std::memcmp(H.magic, "E3DMICRO", 8) != 0 || H.version != 1 || H.nx < 1 || H.ny < 1 || H.nz < 1 ||
+      H.ngrains < 1)
+    return -2;
+  if (nx) *nx = H.nx;
+  if (ny) *ny = H.ny;
+  if (nz) *nz = H.nz;
+  if (ngrains) *ngrains = H.ngrains;
+  return 0;
+}
+
+extern "C" int32_t e3d_micro_read(const char* path, int32_t nx, int32_t ny, int32_t nz, int32_t ngrains,
+                                  int32_t* pix, double* rod) {
+  int32_t hx, hy, hz, hg;
+  int32_t rc = e3d_micro_read_header(path, &hx, &hy, &hz, &hg);
+  if (rc) return rc;
+  // size checks as ppixel_hdf5 (src/elas3dxtal_pcg.f90:2939-2942, 2966-2969)
+  if (hx != nx || hy != ny || hz != nz || hg != ngrains || !pix || !rod) return -2;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return -1;
+  std::fseek(f, (long)sizeof(MicroHeader), SEEK_SET);
+  const size_t ns = (size_t)nx * ny * nz;
+  const bool ok = std::fread(pix, sizeof(int32_t), ns, f) == ns &&
+                  std::fread(rod, sizeof(double), 3 * (size_t)ngrains, f) == 3 * (size_t)ngrains;
+  std::fclose(f);
+  if (!ok) return -2;
+  // phase range (src/elas3dxtal_pcg.f90:2986-2989)
+  for (size_t m = 0; m < ns; ++m)
+    if (pix[m] < 1 || pix[m] > ngrains + 1) return -2;
+  return 0;
 }

@@ -42,7 +42,7 @@ typedef struct e3d_batch_opts {
   int32_t divergence_reset; /* 1: h = z when rel_res grows > 10x                 */
   float tol;                /* single precision, as the reference's tol          */
   int32_t load_cases;       /* bitmask of the six unit load cases (0 = all six)  */
-  int32_t parts;            /* blocks per solve: 0 = autotune                    */
+  int32_t parts;            /* blocks per solve (<= 64): 0 = autotune            */
   int32_t pad;
   double strain;            /* magnitude of the unit load cases (1e-3)           */
   double e1, nu1;           /* inclusion phase modulus / Poisson ratio           */
@@ -92,7 +92,7 @@ typedef struct e3d_serve_opts {
   float tol;
   int32_t max_active;       /* concurrent solves on the device (slots)           */
   int32_t round_iters;      /* PCG iterations per solve per engine round          */
-  int32_t parts;            /* blocks per solve: 0 = by size                      */
+  int32_t parts;            /* blocks per solve (<= 64): 0 = by size              */
   int32_t pad;
   double e1, nu1;
   int64_t hbm_budget;       /* bytes of device memory the server may hold        */

@@ -56,6 +56,10 @@ extern "C" {
 #define E3D_CRIT_REF 0         /* sqrt(z.g / |g0|^2), the reference's test (:1949, :452) */
 #define E3D_CRIT_PRECOND_REL 1 /* sqrt(z.g / z0.g0), true preconditioned relative     */
 
+/* ---- preconditioner ---- */
+#define E3D_PRECOND_BLOCK_JACOBI 0 /* 3x3 point-block Jacobi (dembx_OpenMP, :1498-1535)       */
+#define E3D_PRECOND_NONE 1         /* identity: the plain CG variant (applications/sec3_1/cg) */
+
 /* ---- arithmetic ---- */
 #define E3D_PREC_FP64 0  /* FP64 everywhere (the reference's arithmetic)           */
 #define E3D_PREC_MIXED 1 /* FP32 stencil + preconditioner inside FP64 refinement   */
@@ -71,6 +75,8 @@ typedef struct e3d_problem {
   int32_t device;           /* CUDA device ordinal                                 */
   float tol;                /* single precision, as `real :: tol` (:148)           */
   int32_t refine_every;     /* MIXED: FP64 residual replacement period (0 = 50)    */
+  int32_t preconditioner;   /* E3D_PRECOND_*                                       */
+  int32_t reserved;         /* zero                                                */
   double c11, c12, c44;     /* cubic constants, Pa (:100-102)                      */
   double e1, nu1;           /* inclusion Young's modulus / Poisson ratio (:114-115)*/
   double strain[6];         /* exx, eyy, ezz, exz, eyz, exy (tensor) (:394-399)    */
@@ -166,6 +172,17 @@ int32_t e3d_get_minv(e3d_handle_t* h, double* minv);
 /* Per-iteration rel_res history of the last solve (cgitr file, :2019-2021);
  * copies min(n, iterations) values, returns the count through *count. */
 int32_t e3d_get_history(e3d_handle_t* h, double* hist, int32_t n, int32_t* count);
+
+/* Checkpoint / resume of a solve in progress.  The reference's only resumable
+ * state is e3d%u, gb, h carried across its kkk restart loop
+ * (src/elas3dxtal_pcg.f90:470-508, 2024-2031); here the whole PCG state
+ * (u, g, z, the search direction, scalars, rel_res history; for the mixed form
+ * its FP32 inner state) is written to `path`, so a long solve can stop and
+ * continue in another process.  Save needs a started solve (e3d_solve_begin);
+ * load needs e3d_upload + e3d_femat with the same problem, rebuilds the
+ * preconditioner and continues with e3d_iterate exactly where save stopped. */
+int32_t e3d_checkpoint_save(e3d_handle_t* h, const char* path);
+int32_t e3d_checkpoint_load(e3d_handle_t* h, const char* path);
 
 /* Device pointers of the state vectors (3*ns doubles each, SoA), for callers
  * that keep inputs resident in HBM. */

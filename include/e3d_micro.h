@@ -49,6 +49,21 @@ int32_t e3d_micro_ellipsoidal_pores(int32_t nx, int32_t ny, int32_t nz,
                                     int32_t pore_phase, uint64_t seed,
                                     int32_t* pix);
 
+/* Raw microstructure container (.e3d), the stand-in for the reference's HDF5
+ * input input_structure_poly.h5 (/pix int32 ns, /orientation float64
+ * 3*ngrains; ppixel_hdf5, src/elas3dxtal_pcg.f90:2879-2990) where libhdf5 is
+ * absent.  Little-endian: 8-byte magic "E3DMICRO", int32 version (1), nx, ny,
+ * nz, ngrains, int32 reserved, then pix (ns int32) and rodrigues (3*ngrains
+ * float64).  The reader applies the reference's checks: the sizes must match
+ * (:2939-2942, :2966-2969) and every phase id must lie in [1, ngrains+1]
+ * (:2986-2989).  Return 0 on success, -1 on I/O errors, -2 on a bad file. */
+int32_t e3d_micro_write(const char* path, int32_t nx, int32_t ny, int32_t nz,
+                        int32_t ngrains, const int32_t* pix, const double* rod);
+int32_t e3d_micro_read_header(const char* path, int32_t* nx, int32_t* ny,
+                              int32_t* nz, int32_t* ngrains);
+int32_t e3d_micro_read(const char* path, int32_t nx, int32_t ny, int32_t nz,
+                       int32_t ngrains, int32_t* pix, double* rod);
+
 /* Bunge Euler angles (phi1, Phi, phi2; radians) -> Rodrigues vectors, for
  * callers whose orientation files hold Euler angles.  n orientations. */
 void e3d_euler_to_rodrigues(int32_t n, const double* euler, double* rod);

@@ -617,8 +617,15 @@ int32_t orc_dembx(const orc_problem* p, const int32_t* pix, const int32_t* ib,
   double* z = (double*)malloc(sizeof(double) * n3);
   double* minv = (double*)malloc(sizeof(double) * 9 * ns);
   /* kkk == 1 builds the preconditioner (src/elas3dxtal_pcg.f90:1498-1520);
-   * kmax = 1 in the reference so it is always built here. */
-  orc_block_jacobi(p, pix, ib, dk, minv);
+   * kmax = 1 in the reference so it is always built here.  precond == 1 is the
+   * unpreconditioned CG of applications/sec3_1/cg/n_100x100x100/elas3dxtal_cg.f90:
+   * 1011-1060 (z = g, no divergence reset). */
+  if (p->precond == 1) {
+    memset(minv, 0, sizeof(double) * 9 * ns);
+    for (size_t m = 0; m < ns; ++m) minv[m] = minv[m + 4 * ns] = minv[m + 8 * ns] = 1.0;
+  } else {
+    orc_block_jacobi(p, pix, ib, dk, minv);
+  }
   precond(minv, gb, z, ns);
   double gg = ddot(z, gb, n3);
   if (kkk == 1) memcpy(h, z, sizeof(double) * n3);

@@ -42,6 +42,7 @@ typedef struct orc_problem {
   int32_t criterion;       /* 0 = reference sqrt(z.g/|g0|^2), 1 = sqrt(z.g/z0.g0) */
   int32_t divergence_reset;/* 1 = reset h = z when rel_res jumps > 10x           */
   int32_t block_size;      /* apply chunk (reference: 8192)                       */
+  int32_t precond;         /* 0 block-Jacobi, 1 none (applications/sec3_1/cg)     */
 } orc_problem;
 
 /* Rodrigues -> Bond-rotated cubic stiffness, row-major 36 per grain

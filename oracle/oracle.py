@@ -34,7 +34,7 @@ class OrcProblem(C.Structure):
         ("exx", C.c_double), ("eyy", C.c_double), ("ezz", C.c_double),
         ("exz", C.c_double), ("eyz", C.c_double), ("exy", C.c_double),
         ("tol", C.c_float), ("ldemb", C.c_int32), ("criterion", C.c_int32),
-        ("divergence_reset", C.c_int32), ("block_size", C.c_int32),
+        ("divergence_reset", C.c_int32), ("block_size", C.c_int32), ("precond", C.c_int32),
     ]
 
 
@@ -124,6 +124,7 @@ class Problem:
     criterion: int = 0
     divergence_reset: int = 1
     block_size: int = 8192
+    precond: int = 0
 
     @property
     def ns(self) -> int:
@@ -134,7 +135,7 @@ class Problem:
                           self.c11, self.c12, self.c44, self.e1, self.nu1,
                           self.exx, self.eyy, self.ezz, self.exz, self.eyz, self.exy,
                           self.tol, self.ldemb, self.criterion, self.divergence_reset,
-                          self.block_size)
+                          self.block_size, self.precond)
 
 
 class Oracle:

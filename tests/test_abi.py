@@ -61,6 +61,6 @@ def test_strerror_and_defaults_without_gpu(lib):
 def test_struct_layout_matches_header(lib):
     import ctypes as C
 
-    # e3d_problem_t: 12 int32/float (48 B) + 11 doubles (88 B) + int64 = 144 B
-    assert C.sizeof(e3d.ProblemC) == 144
+    # e3d_problem_t: 14 int32/float (56 B) + 11 doubles (88 B) + int64 = 152 B
+    assert C.sizeof(e3d.ProblemC) == 152
     assert C.sizeof(e3d.SolveStatsC) == 16 + 6 * 8

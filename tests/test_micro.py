@@ -3,6 +3,8 @@
 The seeds and orientations are recomputed here with a Python replica of the
 generator's RNG (xoshiro256** seeded through splitmix64), so the Voronoi
 assignment is checked against brute force."""
+import os
+
 import numpy as np
 import pytest
 
@@ -126,3 +128,28 @@ def test_euler_to_rodrigues_matches_rotation():
 
     for (p1, P, p2), r in zip(eul, rod):
         assert np.allclose(R.rodrigues_to_Q(r), rz(p1) @ rx(P) @ rz(p2), atol=1e-12)
+
+
+def test_e3d_container_roundtrip_and_checks(tmp_path):
+    pix, rod = e3d.micro_grains(9, 8, 7, 5, 2)
+    path = str(tmp_path / "m.e3d")
+    e3d.micro_write(path, pix, rod, (9, 8, 7))
+    p2, r2, shape = e3d.micro_read(path)
+    assert shape == (9, 8, 7) and np.array_equal(p2, pix) and np.array_equal(r2, rod)
+    bad = pix.copy()
+    bad[3] = 7  # ngrains + 2: outside [1, ngrains + 1]
+    e3d.micro_write(path, bad, rod, (9, 8, 7))
+    with pytest.raises(ValueError):
+        e3d.micro_read(path)
+    with open(path, "r+b") as f:  # corrupt the magic
+        f.write(b"XXXX")
+    with pytest.raises(OSError):
+        e3d.micro_read(path)
+
+
+def test_driver_help_runs_without_gpu():
+    import subprocess
+
+    drv = os.path.join(os.path.dirname(e3d.LIB_PATH), "e3d_run")
+    out = subprocess.run([drv, "--help"], capture_output=True, text=True)
+    assert out.returncode == 0 and "--generate" in out.stdout
