@@ -52,7 +52,7 @@ EXPORTED_SYMBOLS = (
     "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
-    "e3d_device_bytes", "e3d_launch_count", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_device_bytes", "e3d_launch_count", "e3d_stencil_path", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
     "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
     "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
@@ -131,6 +131,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_device_bytes.restype = C.c_int64
     L.e3d_launch_count.argtypes = [vp]
     L.e3d_launch_count.restype = C.c_int64
+    L.e3d_stencil_path.argtypes = [vp]
+    L.e3d_stencil_path.restype = C.c_int32
     L.e3d_probe_peaks.argtypes = [C.c_int32, dp, dp]
     L.e3d_apply_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp]
     L.e3d_checkpoint_save.argtypes = [vp, C.c_char_p]
@@ -395,6 +397,10 @@ class Elas3D:
 
     def launch_count(self) -> int:
         return int(self.L.e3d_launch_count(self._h))
+
+    def stencil_path(self) -> str:
+        """'fp64', 'f32' (per-thread loads) or 'f32_tma' (TMA plane ring)."""
+        return ("fp64", "f32", "f32_tma")[int(self.L.e3d_stencil_path(self._h))]
 
 
 def assig(pix: np.ndarray, nphase: int) -> np.ndarray:

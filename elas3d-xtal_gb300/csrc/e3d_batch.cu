@@ -115,7 +115,7 @@ struct JobDev {
 
 size_t rve_bytes(long long ns, int nphase) {
   return align256(4 * ns) + align256(8 * 36 * (size_t)nphase) + align256(8 * kCsStride * (size_t)nphase) +
-         align256(4 * kCsStride * (size_t)nphase) + align256(8 * 576 * (size_t)nphase) +
+         align256(4 * kCs32Stride * (size_t)nphase) + align256(8 * 576 * (size_t)nphase) +
          align256(8 * 72 * (size_t)nphase) + align256(4 * 6 * ns) + align256(sizeof(PhaseMat) * (size_t)nphase);
 }
 
@@ -146,7 +146,7 @@ int32_t setup_rve(RveDev& R, char* base, const e3d_rve_t& in, double e1, double 
   R.pix = carve<int32_t>(p, R.ns);
   R.cmod = carve<double>(p, 36 * (size_t)R.nphase);
   R.cs64 = carve<double>(p, kCsStride * (size_t)R.nphase);
-  R.cs32 = carve<float>(p, kCsStride * (size_t)R.nphase);
+  R.cs32 = carve<float>(p, kCs32Stride * (size_t)R.nphase);
   R.dk = carve<double>(p, 576 * (size_t)R.nphase);
   R.dkd = carve<double>(p, 72 * (size_t)R.nphase);
   R.minv32 = carve<float>(p, 6 * R.ns);

@@ -119,6 +119,113 @@ __device__ __forceinline__ void element_modal(const T* __restrict__ cs, const T 
   fw[0] = T(0);
 }
 
+// FP32 table: the upper triangle of C/16 (row-major, 21 entries, 3 pad), read
+// with six 16-byte loads.  Every Hadamard component belongs to one mode class --
+// first order (HX_, HY_, HZ_) to the constant mode (weight 1/16), second order
+// (HXY, HXZ, HYZ) to the x/y/z modes (1/48 = 1/16 * 1/3), third order (HXYZ) to
+// the xy/xz/yz modes (1/144 = 1/16 * 1/9) -- so scaling the 9 second-order
+// inputs by 1/3 and the 3 third-order inputs by 1/9 lets all seven modes share
+// C/16: 12 multiplies instead of 87 table loads per element.
+constexpr int kCs32Stride = 24;
+
+__host__ __device__ constexpr int sym6(int r, int c) {
+  return r <= c ? r * 6 - r * (r - 1) / 2 + (c - r) : c * 6 - c * (c - 1) / 2 + (r - c);
+}
+
+template <int N>
+__device__ __forceinline__ void matvec_sym(const float (&t)[kCs32Stride], const int (&idx)[N], const float (&e)[N],
+                                           float (&s)[N]) {
+#pragma unroll
+  for (int r = 0; r < N; ++r) {
+    float acc = t[sym6(idx[r], idx[0])] * e[0];
+#pragma unroll
+    for (int c = 1; c < N; ++c) acc = fmaf(t[sym6(idx[r], idx[c])], e[c], acc);
+    s[r] = acc;
+  }
+}
+
+__device__ __forceinline__ void element_modal_f32(const float* __restrict__ cs, const float (&hu)[8],
+                                                  const float (&hv)[8], const float (&hw)[8], float (&fu)[8],
+                                                  float (&fv)[8], float (&fw)[8]) {
+  float t[kCs32Stride];
+  const float4* t4 = reinterpret_cast<const float4*>(cs);
+#pragma unroll
+  for (int i = 0; i < kCs32Stride / 4; ++i) {
+    const float4 q = __ldg(t4 + i);
+    t[4 * i] = q.x;
+    t[4 * i + 1] = q.y;
+    t[4 * i + 2] = q.z;
+    t[4 * i + 3] = q.w;
+  }
+  const float k3 = 1.0f / 3.0f, k9 = 1.0f / 9.0f;
+  const float uxy = hu[HXY] * k3, vxy = hv[HXY] * k3, wxy = hw[HXY] * k3;
+  const float uxz = hu[HXZ] * k3, vxz = hv[HXZ] * k3, wxz = hw[HXZ] * k3;
+  const float uyz = hu[HYZ] * k3, vyz = hv[HYZ] * k3, wyz = hw[HYZ] * k3;
+  const float uxyz = hu[HXYZ] * k9, vxyz = hv[HXYZ] * k9, wxyz = hw[HXYZ] * k9;
+  {
+    const int idx[6] = {0, 1, 2, 3, 4, 5};
+    const float e[6] = {hu[HX_], hv[HY_], hw[HZ_], hu[HZ_] + hw[HX_], hv[HZ_] + hw[HY_], hu[HY_] + hv[HX_]};
+    float s[6];
+    matvec_sym<6>(t, idx, e, s);
+    fu[HX_] = s[0];
+    fv[HY_] = s[1];
+    fw[HZ_] = s[2];
+    fu[HZ_] = s[3];
+    fw[HX_] = s[3];
+    fv[HZ_] = s[4];
+    fw[HY_] = s[4];
+    fu[HY_] = s[5];
+    fv[HX_] = s[5];
+  }
+  float sx[5], sy[5], sz[5];
+  {
+    const int idx[5] = {1, 2, 3, 4, 5};
+    const float e[5] = {vxy, wxz, uxz, vxz + wxy, uxy};
+    matvec_sym<5>(t, idx, e, sx);
+  }
+  {
+    const int idx[5] = {0, 2, 3, 4, 5};
+    const float e[5] = {uxy, wyz, uyz + wxy, vyz, vxy};
+    matvec_sym<5>(t, idx, e, sy);
+  }
+  {
+    const int idx[5] = {0, 1, 3, 4, 5};
+    const float e[5] = {uxz, vyz, wxz, wyz, uyz + vxz};
+    matvec_sym<5>(t, idx, e, sz);
+  }
+  fu[HXY] = sx[4] + sy[0];
+  fv[HXY] = sx[0] + sy[4];
+  fw[HXY] = sx[3] + sy[2];
+  fu[HXZ] = sx[2] + sz[0];
+  fv[HXZ] = sx[3] + sz[4];
+  fw[HXZ] = sx[1] + sz[2];
+  fu[HYZ] = sy[2] + sz[4];
+  fv[HYZ] = sy[3] + sz[1];
+  fw[HYZ] = sy[1] + sz[3];
+  float sxy[3], sxz[3], syz[3];
+  {
+    const int idx[3] = {2, 3, 4};
+    const float e[3] = {wxyz, uxyz, vxyz};
+    matvec_sym<3>(t, idx, e, sxy);
+  }
+  {
+    const int idx[3] = {1, 4, 5};
+    const float e[3] = {vxyz, wxyz, uxyz};
+    matvec_sym<3>(t, idx, e, sxz);
+  }
+  {
+    const int idx[3] = {0, 3, 5};
+    const float e[3] = {uxyz, wxyz, vxyz};
+    matvec_sym<3>(t, idx, e, syz);
+  }
+  fu[HXYZ] = sxy[1] + sxz[2] + syz[0];
+  fv[HXYZ] = sxy[2] + sxz[0] + syz[2];
+  fw[HXYZ] = sxy[0] + sxz[1] + syz[1];
+  fu[0] = 0.f;
+  fv[0] = 0.f;
+  fw[0] = 0.f;
+}
+
 // Forward Hadamard of one plane of 4 corner values v[oy*2+ox] -> P[by*2+bx].
 template <typename T>
 __device__ __forceinline__ void had_xy(const T (&v)[4], T (&P)[4]) {

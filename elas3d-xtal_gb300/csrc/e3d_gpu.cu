@@ -2,6 +2,7 @@
 // replaces one subroutine of src/elas3dxtal_pcg.f90; see the header for the
 // mapping.  All device work runs on the handle's stream; calls return after it
 // completes.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -9,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -32,6 +34,65 @@ struct DevBuf {
 void e3d_record_error_text(const char* text) { g_last_cuda_error = text ? text : ""; }
 void e3d_record_cuda_error(const char* what, cudaError_t e) {
   g_last_cuda_error = std::string(what) + ": " + cudaGetErrorString(e);
+}
+
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver, found through the runtime so the
+// library does not link libcuda (it loads on hosts without a driver).
+EncodeTiledFn encode_tiled_fn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+}  // namespace
+
+// Tensor maps of the TMA-fed FP32 stencil for one grid: 4-D (x, y, z,
+// component) maps of h0, h1 and z with the main / column / row / corner boxes,
+// and a 3-D map of the phase ids.  Needs nx*4 to be a multiple of 16 bytes (the
+// row stride of a tensor map) and 16-byte aligned bases.  Returns false when
+// the grid or the driver does not allow it; the caller then keeps per-thread
+// loads.
+bool e3d_encode_plane_maps(PlaneMaps* out, const float* h0, const float* h1, const float* z, const int32_t* pix,
+                           const GridDims& G) {
+  EncodeTiledFn fn = encode_tiled_fn();
+  if (!fn || G.nx % 4 != 0) return false;
+  for (const void* b : {(const void*)h0, (const void*)h1, (const void*)z, (const void*)pix})
+    if (reinterpret_cast<uintptr_t>(b) % 16 != 0) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)G.nx, (cuuint64_t)G.ny, (cuuint64_t)G.nz, 3};
+  const cuuint64_t strides[3] = {(cuuint64_t)G.nx * 4, (cuuint64_t)G.nx * G.ny * 4, (cuuint64_t)G.ns * 4};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const float* bases[3] = {h0, h1, z};
+  CUtensorMap* dst[3] = {out->h0, out->h1, out->z};
+  for (int v = 0; v < 3; ++v)
+    for (int k = 0; k < 4; ++k) {
+      const cuuint32_t box[4] = {(cuuint32_t)kBoxX[k], (cuuint32_t)kBoxY[k], 1, 3};
+      if (fn(&dst[v][k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(bases[v]), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    }
+  const cuuint32_t pbox[3] = {32, 8, 1};
+  if (fn(&out->pix, CU_TENSOR_MAP_DATA_TYPE_INT32, 3, const_cast<int32_t*>(pix), dims, strides, pbox, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  return true;
 }
 
 struct e3d_handle {
@@ -69,6 +130,9 @@ struct e3d_handle {
   float* Ah32 = nullptr;
   float* minv32 = nullptr;
   int since_replace = 0;
+  // TMA-fed FP32 stencil: tensor maps of h32a, h32b, z32, pix (null: per-thread loads)
+  PlaneMaps* maps = nullptr;
+  int pcg_grid32_tma = 0;
   double* hx = nullptr;
   double* hy = nullptr;
   double* hd = nullptr;
@@ -286,12 +350,20 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
     return fail(cuda_fail(e, "occupancy"));
   if (per_sm32 < 1) return fail(E3D_ERR_CUDA);
   h->pcg_grid32 = per_sm32 * h->num_sms;
+  int per_sm_tma = 0;
+  if (p->precision == E3D_PREC_MIXED) {
+    if ((e = cudaFuncSetAttribute(pcg_persistent_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kRingSmemBytes)) != cudaSuccess ||
+        (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_tma, pcg_persistent_kernel<float, true>, NT,
+                                                           kRingSmemBytes)) != cudaSuccess)
+      return fail(cuda_fail(e, "occupancy (TMA)"));
+  }
   h->partial_n = std::max(std::max(h->pcg_grid, h->pcg_grid32), h->num_sms * 4) * 12;
   const long long halo = h->G.ntiles * h->G.tz;
   int32_t rc = E3D_OK;
   if ((rc = dalloc(h, &h->pix, ns)) || (rc = dalloc(h, &h->rod, 3 * (size_t)std::max(np - 1, 1))) ||
       (rc = dalloc(h, &h->cmod, 36 * (size_t)np)) || (rc = dalloc(h, &h->cs, kCsStride * (size_t)np)) ||
-      (rc = dalloc(h, &h->cs32, kCsStride * (size_t)np)) || (rc = dalloc(h, &h->dk, 576 * (size_t)np)) ||
+      (rc = dalloc(h, &h->cs32, kCs32Stride * (size_t)np)) || (rc = dalloc(h, &h->dk, 576 * (size_t)np)) ||
       (rc = dalloc(h, &h->dkd, 72 * (size_t)np)) || (rc = dalloc(h, &h->u, n3)) || (rc = dalloc(h, &h->g, n3)) ||
       (rc = dalloc(h, &h->b, n3)) || (rc = dalloc(h, &h->z, n3)) || (rc = dalloc(h, &h->h0, n3)) ||
       (rc = dalloc(h, &h->h1, n3)) || (rc = dalloc(h, &h->Ah, n3)) || (rc = dalloc(h, &h->minv, 6 * ns)) ||
@@ -309,6 +381,16 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
     if ((e = cudaMemsetAsync(h->h32a, 0, sizeof(float) * n3, h->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(h->h32b, 0, sizeof(float) * n3, h->stream)) != cudaSuccess)
       return fail(cuda_fail(e, "memset"));
+    // TMA-fed inner stencil where the grid allows it (E3D_NO_TMA=1 keeps per-thread loads)
+    const char* no_tma = std::getenv("E3D_NO_TMA");
+    PlaneMaps hm{};
+    if (!(no_tma && no_tma[0] && no_tma[0] != '0') && per_sm_tma >= 1 &&
+        e3d_encode_plane_maps(&hm, h->h32a, h->h32b, h->z32, h->pix, h->G)) {
+      if ((rc = dalloc(h, &h->maps, 1))) return fail(rc);
+      if ((e = cudaMemcpyAsync(h->maps, &hm, sizeof hm, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+        return fail(cuda_fail(e, "tensor maps"));
+      h->pcg_grid32_tma = std::min(per_sm_tma * h->num_sms, h->pcg_grid32);
+    }
   }
   if ((e = cudaMemsetAsync(h->err, 0, sizeof(int), h->stream)) != cudaSuccess) return fail(cuda_fail(e, "memset"));
   if ((e = cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream)) != cudaSuccess)
@@ -339,6 +421,10 @@ int32_t e3d_destroy(e3d_handle_t* h) {
 
 int64_t e3d_device_bytes(const e3d_handle_t* h) { return h ? h->bytes : 0; }
 int64_t e3d_launch_count(const e3d_handle_t* h) { return h ? h->launches : 0; }
+int32_t e3d_stencil_path(const e3d_handle_t* h) {
+  if (!h || h->prob.precision != E3D_PREC_MIXED) return E3D_PATH_FP64;
+  return h->maps ? E3D_PATH_F32_TMA : E3D_PATH_F32;
+}
 
 int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
   if (!h || !pix) return E3D_ERR_INPUT;
@@ -549,8 +635,11 @@ PcgArgs<float> pcg_args<float>(e3d_handle* h) {
 }
 
 template <typename T>
-int32_t launch_pcg(e3d_handle* h, int it_limit, int grid) {
+int32_t launch_pcg(e3d_handle* h, int it_limit) {
+  const bool tma = sizeof(T) == 4 && h->maps != nullptr;
+  const int grid = sizeof(T) == 8 ? h->pcg_grid : (tma ? h->pcg_grid32_tma : h->pcg_grid32);
   PcgArgs<T> P = pcg_args<T>(h);
+  P.maps = h->maps;
   P.partA = h->partial;
   P.partB = h->partial + grid;
   P.st = h->st;
@@ -561,8 +650,8 @@ int32_t launch_pcg(e3d_handle* h, int it_limit, int grid) {
   P.it_limit = it_limit;
   E3D_CUDA(cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream));
   void* args[] = {&P};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void*)pcg_persistent_kernel<T>, dim3(grid), dim3(NT), args,
-                                              0, h->stream);
+  const void* fn = tma ? (const void*)pcg_persistent_kernel<float, true> : (const void*)pcg_persistent_kernel<T>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NT), args, tma ? kRingSmemBytes : 0, h->stream);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(pcg)");
   return E3D_OK;
@@ -621,7 +710,7 @@ int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
   while (remaining > 0) {
     int chunk = std::min(remaining, 256);
     if (mixed) chunk = std::min(chunk, R - h->since_replace);
-    rc = mixed ? launch_pcg<float>(h, chunk, h->pcg_grid32) : launch_pcg<double>(h, chunk, h->pcg_grid);
+    rc = mixed ? launch_pcg<float>(h, chunk) : launch_pcg<double>(h, chunk);
     if (rc) break;
     if ((rc = read_state(h, &S))) break;
     const int done = S.it;  // iterations so far

@@ -39,7 +39,7 @@ struct JobDesc {
   JumpParams J;
   // shared per RVE (read only)
   const int32_t* pix;  // global phase ids, 0-based into the batch tables
-  const float* cs32;   // [phase][108]
+  const float* cs32;   // [phase][24] packed upper triangle of C/16
   const double* cs64;  // [phase][108]
   const double* dk;    // [phase][576]
   const double* cmod;  // cmod(nphase_total,6,6), Fortran layout
@@ -569,10 +569,10 @@ static __global__ void batch_phase_kernel(const PhaseMat* __restrict__ mats, int
       }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) {
-    cs[(long long)p * kCsStride + i] = csh[i];
-    cs32[(long long)p * kCsStride + i] = (float)csh[i];
-  }
+  for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) cs[(long long)p * kCsStride + i] = csh[i];
+  for (int r = threadIdx.x; r < 6; r += blockDim.x)  // FP32: upper triangle of C/16
+    for (int c = r; c < 6; ++c) cs32[(long long)p * kCs32Stride + sym6(r, c)] = (float)csh[6 * r + c];
+  for (int i = 21 + threadIdx.x; i < kCs32Stride; i += blockDim.x) cs32[(long long)p * kCs32Stride + i] = 0.f;
   if (threadIdx.x < 24) {
     const int cidx = threadIdx.x;
     const int rb = cidx / 3, j = cidx % 3;

@@ -4,13 +4,16 @@
 //   minv                 : 6*ns (symmetric 3x3 block inverse: 00 11 22 01 02 12)
 //   pix                  : ns int32, 0-based phase
 //   cs                   : nphase*108 scaled stiffness (C/16, C/48, C/144)
+//   cs32                 : nphase*24, FP32 upper triangle of C/16 (element_modal_f32)
 //   dk                   : nphase*576, [p][a][i][b][j] (reference local order)
 //   dkd                  : nphase*72 diagonal 3x3 blocks [p][a][i][j]
 //   hx, hy, hd           : tile-edge force halos (see apply_tile)
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 #include "e3d_device.cuh"
+#include "e3d_tma.cuh"
 
 namespace e3d {
 
@@ -26,6 +29,9 @@ constexpr int TILE_Y = 8;
 #endif
 #ifndef E3D_F32_BLOCKS_PER_SM
 #define E3D_F32_BLOCKS_PER_SM 2  // resident 256-thread blocks per SM, FP32 form
+#endif
+#ifndef E3D_TMA_STAGES
+#define E3D_TMA_STAGES 5  // ring stages per block (two in use, the rest in flight), TMA-fed FP32 stencil
 #endif
 constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
 
@@ -68,6 +74,182 @@ struct ApplySmem {
   T node[2][3][(TILE_X + 1) * (TILE_Y + 1)];
   T r[9][NT];
 };
+
+// ---------------------------------------------------------------------------
+// TMA plane ring of the fused FP32 stencil.  One stage holds one node plane of
+// a tile: for h_old and z the main 32x8 box, the +x column box (4x8), the +y
+// row box (32x1) and the corner box (4x1), three components each, then the
+// tile's 32x8 phase ids.  Thread 0 keeps E3D_TMA_STAGES planes in flight,
+// running ahead across the block's tiles; a stage is refilled once every
+// thread has read it (the __syncthreads after each commit), and consumers wait
+// on the stage's mbarrier with a wall-clock limit.
+constexpr int kRingMain = 3 * 32 * 8 * 4;
+constexpr int kRingCol = 3 * 4 * 8 * 4;
+constexpr int kRingRow = 3 * 32 * 1 * 4;
+constexpr int kRingCorner = 3 * 4 * 1 * 4;
+constexpr int kRingVec = kRingMain + kRingCol + kRingRow + 128;  // corner box padded to 128 B
+constexpr int kRingPix = 32 * 8 * 4;
+constexpr int kStageBytes = 2 * kRingVec + kRingPix;
+constexpr unsigned kPlaneTx = 2u * (kRingMain + kRingCol + kRingRow + kRingCorner) + kRingPix;
+constexpr int kRingSmemBytes = E3D_TMA_STAGES * kStageBytes + 128;  // + alignment slack
+static_assert(kRingVec % 128 == 0 && kStageBytes % 128 == 0, "TMA destinations must stay 128-byte aligned");
+
+// Producer state, used by thread 0 only; kept in shared memory so it does not
+// occupy registers of every thread.
+struct RingCursor {
+  long long ptile, tstride, tend;
+  const CUtensorMap* hmap;  // the four maps of the buffer read as h_old
+  int pzl, pzend;
+  unsigned int issued;
+};
+
+struct PlaneRing {
+  unsigned char* stage;   // E3D_TMA_STAGES * kStageBytes, 128-byte aligned
+  uint64_t* full;         // one mbarrier per stage
+  RingCursor* cur;        // shared memory
+  const PlaneMaps* maps;  // tensor maps in global memory
+  int* err;
+  unsigned long long timeout_ns;
+  unsigned int q;  // planes consumed by this block (same in every thread)
+  int failed;      // a wait ran out or an error is flagged: stop waiting and issuing
+};
+
+__device__ __forceinline__ void ring_tile_span(const GridDims& G, long long t, int& zl0, int& zl1) {
+  const int tiz = (int)(t / ((long long)G.ntx * G.nty));
+  const int z0 = tiz * G.tz;
+  zl0 = z0 - 1;
+  zl1 = z0 + min(G.tz, G.nz - z0);
+}
+
+// Warp 0: start the loads of the cursor's next plane into its stage; lane 0
+// sets the expected bytes, lanes 0-8 issue one box each, lane 0 advances the
+// cursor.
+__device__ __forceinline__ void ring_issue(PlaneRing& R, const GridDims& G) {
+  RingCursor& C = *R.cur;
+  const int lane = threadIdx.x;  // warp 0 only
+  // warp-uniform decisions (the cursor was published by the last __syncwarp);
+  // the error flag in global memory is read only on the slow path of a wait
+  const bool bad = __any_sync(0xffffffffu, R.failed);
+  if (bad) R.failed = 1;
+  if (bad || C.ptile >= C.tend) return;
+  const long long t = C.ptile;
+  const int tix = (int)(t % G.ntx);
+  const int tiy = (int)((t / G.ntx) % G.nty);
+  const int x0 = tix * TILE_X, y0 = tiy * TILE_Y;
+  const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0);
+  // +x column / +y row of the tile, wrapped; x starts are multiples of 32 or 0
+  const int xc = (x0 + wx == G.nx) ? 0 : x0 + wx;
+  const int yr = (y0 + wy == G.ny) ? 0 : y0 + wy;
+  const int zp = wrapi(C.pzl, G.nz);
+  const unsigned s = C.issued % E3D_TMA_STAGES;
+  unsigned char* st = R.stage + (size_t)s * kStageBytes;
+  uint64_t* bar = R.full + s;
+  if (lane == 0) mbar_arrive_expect_tx(bar, kPlaneTx);
+  __syncwarp();
+  if (lane < 8) {
+    const int v = lane >> 2, kind = lane & 3;  // vector (h_old, z) and box kind
+    const CUtensorMap* m = (v ? R.maps->z : C.hmap) + kind;
+    const int off = v * kRingVec + (kind == BOX_MAIN ? 0 : kind == BOX_COL ? kRingMain
+                                                   : kind == BOX_ROW ? kRingMain + kRingCol
+                                                                     : kRingMain + kRingCol + kRingRow);
+    const int bx = (kind == BOX_COL || kind == BOX_CORNER) ? xc : x0;
+    const int by = (kind == BOX_ROW || kind == BOX_CORNER) ? yr : y0;
+    tma_load_4d(st + off, m, bx, by, zp, 0, bar);
+  } else if (lane == 8) {
+    tma_load_3d(st + 2 * kRingVec, &R.maps->pix, x0, y0, zp, bar);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    C.issued += 1;
+    if (++C.pzl > C.pzend) {
+      C.ptile += C.tstride;
+      if (C.ptile < C.tend) ring_tile_span(G, C.ptile, C.pzl, C.pzend);
+    }
+  }
+  __syncwarp();
+}
+
+// Once per kernel: barriers, from thread 0; followed by __syncthreads.
+__device__ __forceinline__ void ring_setup(PlaneRing& R, unsigned char* dyn, uint64_t* bars, RingCursor* cur,
+                                           const PlaneMaps* maps, int* err, unsigned long long timeout_ns) {
+  const uint32_t a = smem_u32(dyn);
+  R.stage = dyn + ((128u - (a & 127u)) & 127u);
+  R.full = bars;
+  R.cur = cur;
+  R.maps = maps;
+  R.err = err;
+  R.timeout_ns = timeout_ns;
+  R.q = 0;
+  R.failed = 0;
+  if (threadIdx.x == 0) {
+    cur->ptile = cur->tend = 0;
+    cur->tstride = 1;
+    cur->hmap = maps->h0;
+    cur->pzl = cur->pzend = 0;
+    cur->issued = 0;
+    for (int i = 0; i < E3D_TMA_STAGES; ++i) mbar_init(bars + i, 1);
+    fence_mbar_init();
+  }
+  // (the caller's __syncthreads publishes the cursor and the barriers)
+}
+
+// Start of one stencil pass over tiles first, first+stride, ... < tend, reading
+// h_old through hmap.  Every plane of the previous pass has been consumed.
+__device__ __forceinline__ void ring_begin(PlaneRing& R, const GridDims& G, const CUtensorMap* hmap,
+                                           long long first, long long stride, long long tend) {
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
+      fence_proxy_async_all();  // this block's and (after the grid barrier) the grid's writes before TMA reads
+      RingCursor& C = *R.cur;
+      C.hmap = hmap;
+      C.ptile = first;
+      C.tstride = stride;
+      C.tend = tend;
+      if (first < tend) ring_tile_span(G, first, C.pzl, C.pzend);
+    }
+    __syncwarp();
+    for (int i = 0; i < E3D_TMA_STAGES; ++i) ring_issue(R, G);
+  }
+}
+
+// All threads: wait until plane number n (n - R.q < E3D_TMA_STAGES) has
+// landed; returns its stage.
+__device__ __forceinline__ const unsigned char* ring_wait(PlaneRing& R, unsigned n) {
+  const unsigned s = n % E3D_TMA_STAGES;
+  // fast path: one probe; the slow path polls the error flag and the clock
+  if (!R.failed && !mbar_try_wait(R.full + s, (n / E3D_TMA_STAGES) & 1u)) {
+    if (!mbar_wait(R.full + s, (n / E3D_TMA_STAGES) & 1u, R.timeout_ns, R.err)) {
+      if (*(volatile int*)R.err == DEV_OK) atomicExch(R.err, DEV_TIMEOUT);
+      R.failed = 1;
+    }
+  }
+  return R.stage + (size_t)s * kStageBytes;
+}
+
+// Stage address of plane number n (already waited for).
+__device__ __forceinline__ const unsigned char* ring_stage(const PlaneRing& R, unsigned n) {
+  return R.stage + (size_t)(n % E3D_TMA_STAGES) * kStageBytes;
+}
+
+// All threads, after a __syncthreads that follows every read of the oldest
+// plane R.q: its stage is free (the barrier orders those reads before the
+// refill); warp 0 refills it with the cursor's next plane.
+__device__ __forceinline__ void ring_release(PlaneRing& R, const GridDims& G) {
+  R.q += 1;
+  if (threadIdx.x < 32) ring_issue(R, G);
+}
+
+// Thread 0, before the block exits: wait (bounded) for the last plane issued
+// into each stage, so that no copy is still in flight after a failed pass.
+// Phases complete in order, so the last one covers the earlier ones.
+__device__ __forceinline__ void ring_drain(PlaneRing& R) {
+  if (threadIdx.x != 0) return;
+  const unsigned issued = R.cur->issued;
+  for (unsigned s = 0; s < E3D_TMA_STAGES && s < issued; ++s) {
+    const unsigned n = s + E3D_TMA_STAGES * ((issued - 1 - s) / E3D_TMA_STAGES);
+    (void)mbar_wait(R.full + s, (n / E3D_TMA_STAGES) & 1u, 1000000000ull);
+  }
+}
 
 // One tile: TILE_X x TILE_Y element columns marching through tz element planes
 // (plus one redundant plane below).  Each thread owns node column (x0+tx,
@@ -177,28 +359,38 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
     }
   };
 
-  T cur[3][4], Pold[3][4], carry[3][4];
+  T Pold[3][4], carry[3][4];
+  // FP32: the tile's share of h.Ah is summed in FP32 and added to the FP64
+  // accumulator once per tile; FP64: every node's term goes straight into it.
+  float dot32 = 0.f;
+  auto add_dot = [&](T v) {
+    if constexpr (sizeof(T) == 4)
+      dot32 += v;
+    else
+      hAh += (double)v;
+  };
   const long long ecol = (long long)xg + (long long)G.nx * yg;  // element column
   prefetch(z0 - 1);
   commit(z0 - 1, false);
   __syncthreads();
   if (active) {
-    read_corners(z0 - 1, cur);
+    T v0[3][4];
+    read_corners(z0 - 1, v0);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) had_xy(cur[c], Pold[c]);
+    for (int c = 0; c < 3; ++c) had_xy(v0[c], Pold[c]);
   }
   prefetch(z0);
-  int ph_cur = active ? __ldg(A.pix + ecol + nxy * wrapi(z0 - 1, G.nz)) : 0;
+  int ph_cur = active ? __ldcs(A.pix + ecol + nxy * wrapi(z0 - 1, G.nz)) : 0;
   const int htiles_stride = G.tz;  // per-tile plane stride in halo buffers
   for (int k = z0 - 1; k < z0 + wz; ++k) {
     const bool own_next = (k + 1 >= z0) && (k + 1 < z0 + wz);
     commit(k + 1, own_next);
     __syncthreads();
     if (k + 2 <= z0 + wz) prefetch(k + 2);
-    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldg(A.pix + ecol + nxy * wrapi(k + 1, G.nz)) : 0;
+    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldcs(A.pix + ecol + nxy * wrapi(k + 1, G.nz)) : 0;
     T rr[3][4];
-    T nxt[3][4];
     if (active) {
+      T nxt[3][4];
       read_corners(k + 1, nxt);
       T Pn[3][4];
       T h[3][8];
@@ -212,7 +404,10 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         }
       }
       T f[3][8];
-      element_modal<T>(A.cs + (long long)ph_cur * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
+      if constexpr (sizeof(T) == 4)
+        element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+      else
+        element_modal<T>(A.cs + (long long)ph_cur * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         T lo[4];
@@ -226,6 +421,21 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         if (k >= z0) had_xy_adj(lo, rr[c]);
 #pragma unroll
         for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+      }
+    }
+    // plane k's values for the dot products, read before the barrier below
+    // (after it, the next step may overwrite this buffer with plane k+2)
+    T hk[3][4];
+    if (k >= z0 && active) {
+      const T* cb = sm.node[(k + 2) & 1][0];
+      constexpr int cst = (TILE_X + 1) * (TILE_Y + 1);
+      const int o = ty * (TILE_X + 1) + tx;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        hk[c][0] = cb[c * cst + o];
+        hk[c][1] = tx == wx - 1 ? cb[c * cst + o + 1] : T(0);
+        hk[c][2] = ty == wy - 1 ? cb[c * cst + o + TILE_X + 1] : T(0);
+        hk[c][3] = (tx == wx - 1 && ty == wy - 1) ? cb[c * cst + o + TILE_X + 2] : T(0);
       }
     }
     if (k >= z0) {
@@ -253,33 +463,211 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
           hyv[c] = rr[c][2] + (tx > 0 ? sm.r[3 * c + 2][tid - 1] : T(0));
         }
         // per-node dot in T, accumulated in FP64
-        hAh += (double)(cur[0][0] * acc[0] + cur[1][0] * acc[1] + cur[2][0] * acc[2]);
+        add_dot(hk[0][0] * acc[0] + hk[1][0] * acc[1] + hk[2][0] * acc[2]);
         const long long hb = tile * htiles_stride + lz;
         if (tx == wx - 1) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty] = hxv[c];
-          hAh += (double)(cur[0][1] * hxv[0] + cur[1][1] * hxv[1] + cur[2][1] * hxv[2]);
+          add_dot(hk[0][1] * hxv[0] + hk[1][1] * hxv[1] + hk[2][1] * hxv[2]);
         }
         if (ty == wy - 1) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx] = hyv[c];
-          hAh += (double)(cur[0][2] * hyv[0] + cur[1][2] * hyv[1] + cur[2][2] * hyv[2]);
+          add_dot(hk[0][2] * hyv[0] + hk[1][2] * hyv[1] + hk[2][2] * hyv[2]);
         }
         if (tx == wx - 1 && ty == wy - 1) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * htiles_stride + hb] = rr[c][3];
-          hAh += (double)(cur[0][3] * rr[0][3] + cur[1][3] * rr[1][3] + cur[2][3] * rr[2][3]);
+          add_dot(hk[0][3] * rr[0][3] + hk[1][3] * rr[1][3] + hk[2][3] * rr[2][3]);
         }
       }
     }
+    ph_cur = ph_nxt;
+  }
+  if constexpr (sizeof(T) == 4) hAh += (double)dot32;
+}
+
+// Shared memory of apply_tile_ring: the in-plane force exchange, double-buffered
+// by plane parity so one barrier per plane suffices.
+struct RingApplySmem {
+  float r[2][9][NT];
+};
+
+// The fused FP32 tile fed by the plane ring (TMA).  Same element arithmetic,
+// values and summation order as apply_tile<float, true> -- the results are
+// bitwise the same -- but every thread reads its element's four corners of
+// plane k+1 straight from the ring stage (main box, or the +x column / +y row /
+// corner box at the tile edge) and forms h_new = z + gamma*h_old there, so no
+// node buffer and no copy barrier are needed; with the force exchange
+// double-buffered one __syncthreads per plane orders the steps, and the oldest
+// stage is refilled right after it.  Plane k uses ring planes R.q (k) and R.q+1
+// (k+1).
+static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile, RingApplySmem& sm, double& hAh,
+                                PlaneRing& R) {
+  const GridDims& G = A.g;
+  const int tid = threadIdx.x;
+  const int tx = tid % TILE_X, ty = tid / TILE_X;
+  const int tix = (int)(tile % G.ntx);
+  const int tiy = (int)((tile / G.ntx) % G.nty);
+  const int tiz = (int)(tile / ((long long)G.ntx * G.nty));
+  const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+  const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+  const bool active = (tx < wx) && (ty < wy);
+  const long long ns = G.ns;
+  const long long nxy = (long long)G.nx * G.ny;
+  const long long ncol = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+  // stage offset (floats within one vector) and component stride of corner d
+  // = dx + 2*dy of this thread's element
+  auto corner_at = [&](int d, int& off, int& str) {
+    const int lx = tx + (d & 1), ly = ty + (d >> 1);
+    if (lx < wx) {
+      if (ly < wy) {
+        off = ly * TILE_X + lx;
+        str = NT;
+      } else {
+        off = (kRingMain + kRingCol) / 4 + lx;
+        str = TILE_X;
+      }
+    } else {
+      if (ly < wy) {
+        off = kRingMain / 4 + ly * 4;
+        str = TILE_X;
+      } else {
+        off = (kRingMain + kRingCol + kRingRow) / 4;
+        str = 4;
+      }
+    }
+  };
+  auto hval = [&](const unsigned char* st, int off) -> float {
+    const float x = reinterpret_cast<const float*>(st)[off];
+    const float z = reinterpret_cast<const float*>(st + kRingVec)[off];
+    return A.reset ? z : fmaf(A.gamma, x, z);
+  };
+  auto corners = [&](const unsigned char* st, float (&v)[3][4]) {
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+      int off, str;
+      corner_at(d, off, str);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c][d] = hval(st, off + c * str);
+    }
+  };
+  auto phase_of = [&](const unsigned char* st) { return reinterpret_cast<const int*>(st + 2 * kRingVec)[tid]; };
+
+  float Pold[3][4], carry[3][4];
+  float dot32 = 0.f;
+  int ph_cur = 0;
+  {
+    const unsigned char* st = ring_wait(R, R.q);  // plane z0-1
     if (active) {
+      float v0[3][4];
+      corners(st, v0);
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
+      for (int c = 0; c < 3; ++c) had_xy(v0[c], Pold[c]);
+      ph_cur = phase_of(st);
+    }
+  }
+  const int hstride = G.tz;
+  for (int k = z0 - 1; k < z0 + wz; ++k) {
+    const unsigned char* st1 = ring_wait(R, R.q + 1);  // plane k+1
+    float rr[3][4];
+    int ph_nxt = 0;
+    if (active) {
+      float nxt[3][4];
+      corners(st1, nxt);
+      if (k + 1 >= z0 && k + 1 < z0 + wz) {
+        const long long m = ncol + nxy * (k + 1);
 #pragma unroll
-        for (int b = 0; b < 4; ++b) cur[c][b] = nxt[c][b];
+        for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = nxt[c][0];
+      }
+      ph_nxt = phase_of(st1);
+      float Pn[3][4], h[3][8];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        had_xy(nxt[c], Pn[c]);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          h[c][b] = Pn[c][b] + Pold[c][b];
+          h[c][b + 4] = Pn[c][b] - Pold[c][b];
+        }
+      }
+      float f[3][8];
+      element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float lo[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          lo[b] = f[c][b] - f[c][b + 4];
+          const float hi = f[c][b] + f[c][b + 4];
+          if (k >= z0) lo[b] += carry[c][b];
+          carry[c][b] = hi;
+        }
+        if (k >= z0) had_xy_adj(lo, rr[c]);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+      }
+    }
+    // plane k's h_new for the dot products, read before the barrier (the
+    // stage is refilled after it)
+    float hk[3][4];
+    if (k >= z0 && active) {
+      const unsigned char* st0 = ring_stage(R, R.q);
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        const bool need = d == 0 || (d == 1 && tx == wx - 1) || (d == 2 && ty == wy - 1) ||
+                          (d == 3 && tx == wx - 1 && ty == wy - 1);
+        int off, str;
+        corner_at(d, off, str);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hk[c][d] = need ? hval(st0, off + c * str) : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sm.r[k & 1][3 * c + 0][tid] = rr[c][1];  // to node (x+1, y)
+        sm.r[k & 1][3 * c + 1][tid] = rr[c][2];  // to node (x, y+1)
+        sm.r[k & 1][3 * c + 2][tid] = rr[c][3];  // to node (x+1, y+1)
+      }
+    }
+    __syncthreads();
+    ring_release(R, G);  // plane k
+    if (k >= z0 && active) {
+      const float(*r)[NT] = sm.r[k & 1];
+      const int lz = k - z0;
+      const long long m = ncol + nxy * k;
+      float hxv[3], hyv[3], acc[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        acc[c] = rr[c][0];
+        if (tx > 0) acc[c] += r[3 * c + 0][tid - 1];
+        if (ty > 0) acc[c] += r[3 * c + 1][tid - TILE_X];
+        if (tx > 0 && ty > 0) acc[c] += r[3 * c + 2][tid - TILE_X - 1];
+        A.y[m + c * ns] = acc[c];
+        hxv[c] = rr[c][1] + (ty > 0 ? r[3 * c + 2][tid - TILE_X] : 0.f);
+        hyv[c] = rr[c][2] + (tx > 0 ? r[3 * c + 2][tid - 1] : 0.f);
+      }
+      dot32 += hk[0][0] * acc[0] + hk[1][0] * acc[1] + hk[2][0] * acc[2];
+      const long long hb = tile * hstride + lz;
+      if (tx == wx - 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * hstride + hb) * TILE_Y + ty] = hxv[c];
+        dot32 += hk[0][1] * hxv[0] + hk[1][1] * hxv[1] + hk[2][1] * hxv[2];
+      }
+      if (ty == wy - 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * hstride + hb) * TILE_X + tx] = hyv[c];
+        dot32 += hk[0][2] * hyv[0] + hk[1][2] * hyv[1] + hk[2][2] * hyv[2];
+      }
+      if (tx == wx - 1 && ty == wy - 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * hstride + hb] = rr[c][3];
+        dot32 += hk[0][3] * rr[0][3] + hk[1][3] * rr[1][3] + hk[2][3] * rr[2][3];
+      }
     }
     ph_cur = ph_nxt;
   }
+  ring_release(R, G);  // plane z0+wz, last read before the final step's barrier
+  hAh += (double)dot32;
 }
 
 // Halo contribution for node (x, y, z) from the neighbouring tiles.
@@ -530,10 +918,10 @@ static __global__ void femat_phase_kernel(FematParams P, const double* __restric
       }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) {
-    cs[(long long)p * kCsStride + i] = csh[i];
-    cs32[(long long)p * kCsStride + i] = (float)csh[i];
-  }
+  for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) cs[(long long)p * kCsStride + i] = csh[i];
+  for (int r = threadIdx.x; r < 6; r += blockDim.x)  // FP32: upper triangle of C/16
+    for (int c = r; c < 6; ++c) cs32[(long long)p * kCs32Stride + sym6(r, c)] = (float)csh[6 * r + c];
+  for (int i = 21 + threadIdx.x; i < kCs32Stride; i += blockDim.x) cs32[(long long)p * kCs32Stride + i] = 0.f;
   // dk columns: K applied to unit nodal vectors with the same element routine
   // as the stencil, so the preconditioner and b see exactly that matrix.
   if (threadIdx.x < 24) {
@@ -944,13 +1332,25 @@ struct PcgArgs {
   int* err;
   int it_limit;
   unsigned long long timeout_ns;
+  const PlaneMaps* maps;  // TMA form only
 };
 
-template <typename T>
+// TMA (FP32 only): phase A reads its node planes through the block's plane
+// ring (dynamic shared memory of kRingSmemBytes).
+template <typename T, bool TMA = false>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1) pcg_persistent_kernel(PcgArgs<T> P) {
-  __shared__ ApplySmem<T> sm;
+  static_assert(!TMA || sizeof(T) == 4, "the plane ring feeds the FP32 stencil");
+  using Smem = std::conditional_t<TMA, RingApplySmem, ApplySmem<T>>;
+  __shared__ Smem sm;
   __shared__ double red[NT / 32];
   __shared__ PcgState S0;
+  __shared__ uint64_t ring_bars[E3D_TMA_STAGES];
+  __shared__ RingCursor ring_cur;
+  PlaneRing ring;
+  if constexpr (TMA) {
+    extern __shared__ __align__(128) unsigned char e3d_ring_smem[];
+    ring_setup(ring, e3d_ring_smem, ring_bars, &ring_cur, P.maps, P.err, P.timeout_ns);
+  }
   if (threadIdx.x == 0) S0 = *P.st;
   __syncthreads();
   PcgState s = S0;
@@ -968,14 +1368,19 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     A.gamma = (T)s.gamma;
     A.reset = s.reset;
     double hAh_t = 0.0;
+    if constexpr (TMA) ring_begin(ring, G, s.cur ? P.maps->h1 : P.maps->h0, blockIdx.x, gridDim.x, G.ntiles);
     for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
-      apply_tile<T, true>(A, t, sm, hAh_t);
+      if constexpr (TMA)
+        apply_tile_ring(A, t, sm, hAh_t, ring);
+      else
+        apply_tile<T, true>(A, t, sm, hAh_t);
       __syncthreads();
     }
     {
       const double bs = block_sum<NT>(hAh_t, red);
       if (threadIdx.x == 0) P.partA[blockIdx.x] = bs;
     }
+    if constexpr (TMA) fence_proxy_async_all();  // h_new stores before the next pass's TMA reads
     if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
       s.status = PCG_TIMEOUT;
       break;
@@ -1010,6 +1415,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
         const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
         if (tx >= wx || ty >= wy) continue;
         const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+        float zg32 = 0.f;  // FP32: this column's z.g, added to the FP64 sum once per tile
         for (int lz0 = 0; lz0 < wz; lz0 += U) {
           T ah[U][3], hv[U][3], uv[U][3], gv[U][3], mi[U][6];
 #pragma unroll
@@ -1045,16 +1451,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
               P.z[m] = z0v;
               P.z[m + ns] = z1v;
               P.z[m + 2 * ns] = z2v;
-              zg_t += (double)(z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2]);
+              if constexpr (sizeof(T) == 4)
+                zg32 += z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2];
+              else
+                zg_t += (double)(z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2]);
             }
           }
         }
+        if constexpr (sizeof(T) == 4) zg_t += (double)zg32;
       }
     }
     {
       const double bs = block_sum<NT>(zg_t, red);
       if (threadIdx.x == 0) P.partB[blockIdx.x] = bs;
     }
+    if constexpr (TMA) fence_proxy_async_all();  // z stores before the next pass's TMA reads
     if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
       s.status = PCG_TIMEOUT;
       break;
@@ -1083,6 +1494,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     }
   }
   if (s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+  if constexpr (TMA) ring_drain(ring);
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.st = s;
 }
 

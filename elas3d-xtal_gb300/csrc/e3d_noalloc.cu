@@ -17,6 +17,7 @@
 // the table and halos are fully rewritten before they are read.  Calls that
 // overlap on the GPU (other streams, other host threads, same device) race on
 // the array and must be serialised by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -194,6 +194,13 @@ int64_t e3d_device_bytes(const e3d_handle_t* h);
 /* Number of kernel launches issued by the handle so far. */
 int64_t e3d_launch_count(const e3d_handle_t* h);
 
+/* Which inner stencil the solve runs: E3D_PATH_FP64 (plain FP64 form),
+ * E3D_PATH_F32 (mixed form, per-thread loads) or E3D_PATH_F32_TMA (mixed form,
+ * node planes staged in shared memory by TMA; grids with nx % 4 == 0 unless
+ * the environment sets E3D_NO_TMA=1 when the handle is created). */
+enum { E3D_PATH_FP64 = 0, E3D_PATH_F32 = 1, E3D_PATH_F32_TMA = 2 };
+int32_t e3d_stencil_path(const e3d_handle_t* h);
+
 /* No counterpart in the reference.  y = K x, the same matrix-free stencil as
  * e3d_apply_device, for callers that must not allocate device memory: a host
  * framework that owns every device allocation and forbids library-side
