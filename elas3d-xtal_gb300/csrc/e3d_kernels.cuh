@@ -1351,24 +1351,29 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     extern __shared__ __align__(128) unsigned char e3d_ring_smem[];
     ring_setup(ring, e3d_ring_smem, ring_bars, &ring_cur, P.maps, P.err, P.timeout_ns);
   }
-  if (threadIdx.x == 0) S0 = *P.st;
+  // The PCG scalars live in shared memory: every thread reads them after a
+  // barrier, thread 0 alone updates them (all blocks compute the same values
+  // from the same partials), so they hold no registers during the sweeps.
+  PcgState& s = S0;
+  if (threadIdx.x == 0) s = *P.st;
   __syncthreads();
-  PcgState s = S0;
   if (s.status != PCG_RUNNING) return;
+  const bool lead = threadIdx.x == 0;
   const GridDims& G = P.A.g;
   const long long ns = G.ns;
   const int it_end = min(s.it + P.it_limit, s.max_iter);
   while (s.it < it_end) {
     // ---- phase A: fused direction update + stencil + h.Ah
     ApplyArgs<T> A = P.A;
-    A.x = s.cur ? P.h1 : P.h0;
-    A.hnew = s.cur ? P.h0 : P.h1;
+    const int cur = s.cur;
+    A.x = cur ? P.h1 : P.h0;
+    A.hnew = cur ? P.h0 : P.h1;
     A.zv = P.z;
     A.y = P.Ah;
     A.gamma = (T)s.gamma;
     A.reset = s.reset;
     double hAh_t = 0.0;
-    if constexpr (TMA) ring_begin(ring, G, s.cur ? P.maps->h1 : P.maps->h0, blockIdx.x, gridDim.x, G.ntiles);
+    if constexpr (TMA) ring_begin(ring, G, cur ? P.maps->h1 : P.maps->h0, blockIdx.x, gridDim.x, G.ntiles);
     for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
       if constexpr (TMA)
         apply_tile_ring(A, t, sm, hAh_t, ring);
@@ -1382,26 +1387,26 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     }
     if constexpr (TMA) fence_proxy_async_all();  // h_new stores before the next pass's TMA reads
     if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
-      s.status = PCG_TIMEOUT;
+      if (lead) s.status = PCG_TIMEOUT;
       break;
     }
     const double hAh = reduce_broadcast(P.partA, gridDim.x, red);
-    s.it += 1;
-    s.cur ^= 1;
-    s.hAh = hAh;
-    if (!isfinite(hAh)) {
-      s.status = PCG_BREAKDOWN;
-      break;
+    if (lead) {
+      s.it += 1;
+      s.cur ^= 1;
+      s.hAh = hAh;
+      if (!isfinite(hAh))
+        s.status = PCG_BREAKDOWN;
+      else if (fabs(hAh) < 1e-14)  // src/elas3dxtal_pcg.f90:1899-1902
+        s.status = PCG_HAH;
     }
-    if (fabs(hAh) < 1e-14) {  // src/elas3dxtal_pcg.f90:1899-1902
-      s.status = PCG_HAH;
-      break;
-    }
+    __syncthreads();
+    if (s.status != PCG_RUNNING) break;
     const double lambda = s.gg / hAh;
     const T lam = (T)lambda;
     // ---- phase B: u, g update, preconditioner, z.g -- node loop in tile order
     // (no index division), z unrolled so several nodes' loads are in flight.
-    const T* hc = s.cur ? P.h1 : P.h0;
+    const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
     double zg_t = 0.0;
     {
       constexpr int U = sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64;
@@ -1467,33 +1472,36 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     }
     if constexpr (TMA) fence_proxy_async_all();  // z stores before the next pass's TMA reads
     if (!grid_barrier(P.bar, P.err, P.timeout_ns)) {
-      s.status = PCG_TIMEOUT;
+      if (lead) s.status = PCG_TIMEOUT;
       break;
     }
-    const double gglast = s.gg;
-    s.gg = reduce_broadcast(P.partB, gridDim.x, red);
-    s.gglast = gglast;
-    if (!isfinite(s.gg)) {
-      s.status = PCG_BREAKDOWN;
-      break;
+    const double gg_new = reduce_broadcast(P.partB, gridDim.x, red);
+    if (lead) {
+      const double gglast = s.gg;
+      s.gg = gg_new;
+      s.gglast = gglast;
+      if (!isfinite(gg_new)) {
+        s.status = PCG_BREAKDOWN;
+      } else {
+        const double rel_res = sqrt(gg_new / s.gg0);
+        s.rel_res = rel_res;
+        if (blockIdx.x == 0 && P.history) P.history[s.it - 1] = rel_res;
+        if (s.divergence_reset && rel_res > 10.0 * s.rel_res_prev && s.it > 1) {  // :1961-1981
+          s.reset = 1;
+          s.resets += 1;
+        } else {
+          s.gamma = gg_new / gglast;
+          s.reset = 0;
+        }
+        s.rel_res_prev = rel_res;
+        if (rel_res < s.tol) s.status = PCG_CONVERGED;
+      }
     }
-    const double rel_res = sqrt(s.gg / s.gg0);
-    s.rel_res = rel_res;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && P.history) P.history[s.it - 1] = rel_res;
-    if (s.divergence_reset && rel_res > 10.0 * s.rel_res_prev && s.it > 1) {
-      s.reset = 1;
-      s.resets += 1;
-    } else {
-      s.gamma = s.gg / gglast;
-      s.reset = 0;
-    }
-    s.rel_res_prev = rel_res;
-    if (rel_res < s.tol) {
-      s.status = PCG_CONVERGED;
-      break;
-    }
+    __syncthreads();
+    if (s.status != PCG_RUNNING) break;
   }
-  if (s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+  __syncthreads();
+  if (lead && s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
   if constexpr (TMA) ring_drain(ring);
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.st = s;
 }
