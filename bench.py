@@ -36,6 +36,8 @@ PKG_DIR = os.path.join(ROOT, "elas3d-xtal_gb300")
 METRIC = "DOF-iters/s (plain FP64 PCG, 500^3 polycrystal)"
 UNIT = "DOF-iter/s"
 BYTES_PER_NODE_ITER = 364.0   # algorithmic HBM bytes per node per PCG iteration (FP64)
+BYTES_PER_NODE_ITER_MIXED = 184.0  # the same with FP32 vectors, int32 phases and FP32 Minv (mixed inner loop)
+METRIC_MIXED = "DOF-iters/s (mixed-precision PCG inner loop incl. FP64 replacement, 500^3 polycrystal)"
 FLOPS_PER_NODE_ITER = 1200.0  # algorithmic flops per node per PCG iteration (dense stencil)
 
 
@@ -117,10 +119,11 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic_per_node():
+def _traffic_per_node(mixed: bool = False):
     """DRAM bytes per node per iteration of the PCG kernel from the committed
-    ncu capture summary (profiles/pcg_fp64_traffic.json), if present."""
-    path = os.path.join(ROOT, "profiles", "pcg_fp64_traffic.json")
+    ncu capture summary (profiles/pcg_fp64_traffic.json, or pcg_f32_traffic.json
+    for the mixed inner loop), if present."""
+    path = os.path.join(ROOT, "profiles", "pcg_f32_traffic.json" if mixed else "pcg_fp64_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
@@ -238,8 +241,14 @@ def run_ours(args):
     e3d = _load_package()
     p, pix, rod = _workload(args.n)
     p.device = local
+    mixed = args.precision == "mixed"
+    if mixed:
+        p.precision = e3d.PREC_MIXED
+        p.refine_every = 50
     K, Wm = args.steps, args.warmup
     ns = p.ns
+    metric = METRIC_MIXED if mixed else METRIC
+    bytes_node = BYTES_PER_NODE_ITER_MIXED if mixed else BYTES_PER_NODE_ITER
 
     # ---- device-resident measurement
     g = e3d.Elas3D(p)
@@ -247,6 +256,7 @@ def run_ours(args):
     g.energy()
     g.solve_begin()
     st = g.iterate(Wm)
+    path = g.stencil_path()
     it0, ms0, l0 = st["iterations"], st["ms_iter"], g.launch_count()
     _barrier(pg)
     clocks = ClockSampler(local).start()
@@ -306,31 +316,34 @@ def run_ours(args):
     # ---- roofline of the dominant kernel (pcg_persistent_kernel)
     hbm, hbm_src = _peaks()
     t_iter = ms / 1e3 / K
-    achieved = BYTES_PER_NODE_ITER * ns / t_iter / 1e9
-    traffic_node, fp64_inst_node = _traffic_per_node()
+    achieved = bytes_node * ns / t_iter / 1e9
+    traffic_node, fp64_inst_node = _traffic_per_node(mixed)
     fp64_peak, fp32_peak = e3d.probe_peaks(local)
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json)",
             "traffic": traffic_node * ns if traffic_node else None,
-            "kernel": "pcg_persistent_kernel (one PCG iteration)",
-            "algorithmic_bytes_per_node": BYTES_PER_NODE_ITER}
+            "kernel": f"pcg_persistent_kernel<{'float' if mixed else 'double'}> (one PCG iteration; stencil path {path})",
+            "algorithmic_bytes_per_node": bytes_node}
     comp = {"bound": "fp64", "peak_tflops": fp64_peak, "peak_source": "measured DFMA probe (e3d_probe_peaks)",
             "fp32_peak_tflops": fp32_peak,
             "algorithmic_tflops_dense_equiv": FLOPS_PER_NODE_ITER * ns / t_iter / 1e12}
-    if fp64_inst_node:
+    if fp64_inst_node and not mixed:
         # executed FP64 instructions (ncu), each FMA counted as 2 flops at most
         comp["executed_fp64_inst_per_node"] = fp64_inst_node
         comp["executed_fp64_inst_per_s"] = fp64_inst_node * ns / t_iter
         comp["frac_of_fp64_issue_peak"] = fp64_inst_node * ns / t_iter / (fp64_peak * 1e12 / 2.0)
-    roof["fp64_pipe"] = comp
+    if not mixed:
+        roof["fp64_pipe"] = comp
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": Wm,
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": Wm,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded generator, shapes/distributions of the 500^3 config)",
+        "dtype": "f32 (FP64 dots, scalars and residual replacement)" if mixed else "f64",
+        "data": "synthetic (seeded generator, shapes/distributions of the 500^3 config)",
         "config": {"workload": f"c2_polycrystal_{args.n}", "grid": [args.n] * 3, "dof": 3 * ns,
                    "grains": p.nphase - 1, "zener_A": 2.0, "pores": "1% spherical, r ~ lognormal(ln 3, 0.4)",
-                   "precision": "fp64", "criterion": "reference (sqrt(z.g/|g0|^2))",
+                   "precision": "mixed (FP64 residual replacement every 50 iterations)" if mixed else "fp64",
+                   "stencil_path": path, "criterion": "reference (sqrt(z.g/|g0|^2))",
                    "step": "one PCG iteration (fused apply + updates, persistent kernel)",
                    "l2": "inputs larger than L2 (3 GB per vector)", "parallelism": f"replicas x{ws}",
                    "e2e": "C-ABI calls from pinned host buffers: upload..K iterations..stress, get_u"},
@@ -531,6 +544,8 @@ def main():
     ap.add_argument("--n", type=int, default=500, help="grid edge (default: the 500^3 config)")
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+                    help="plain form: the FP64 PCG (default) or the mixed-precision inner loop")
     ap.add_argument("--form", choices=["plain", "solve", "batch", "serve"], default="plain",
                     help="plain: the FP64 DOF-iters/s line; solve/batch/serve: the added forms")
     ap.add_argument("--rves", type=int, default=256, help="batch: ensemble size")
