@@ -291,26 +291,38 @@ static __device__ void job_fold(const JobDesc& J, int part) {
 #ifndef E3D_ENGINE_BLOCKS_PER_SM
 #define E3D_ENGINE_BLOCKS_PER_SM 2  // resident engine blocks per SM (register budget)
 #endif
+// The part's job descriptor and PCG scalars live in shared memory: thread 0
+// writes them, every thread reads them after a barrier, so neither occupies
+// registers during the sweeps.
 static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engine_kernel(EngineArgs E) {
   __shared__ __align__(16) unsigned char smraw[sizeof(ApplySmem<double>)];
   __shared__ double red[NT / 32];
-  __shared__ int s_idx;
+  __shared__ int s_idx, s_part;
+  __shared__ JobDesc sJ;
+  __shared__ PcgState sS;
   ApplySmem<double>& sm64 = *reinterpret_cast<ApplySmem<double>*>(smraw);
   ApplySmem<float>& sm32 = *reinterpret_cast<ApplySmem<float>*>(smraw);
   const unsigned long long to = E.timeout_ns;
+  const bool lead = threadIdx.x == 0;
+  const JobDesc& J = sJ;
+  PcgState& s = sS;
   for (;;) {
-    if (threadIdx.x == 0) s_idx = (int)atomicAdd(E.head, 1u);
+    __syncthreads();  // the previous part is done with sJ / sS
+    if (lead) {
+      const int idx = (int)atomicAdd(E.head, 1u);
+      s_idx = idx;
+      if (idx < E.nparts_total) {
+        sJ = E.jobs[E.part_job[idx]];
+        s_part = E.part_rank[idx];
+      }
+    }
     __syncthreads();
-    const int idx = s_idx;
-    __syncthreads();
-    if (idx >= E.nparts_total) break;
-    const JobDesc J = E.jobs[E.part_job[idx]];
-    const int part = E.part_rank[idx];
+    if (s_idx >= E.nparts_total) break;
+    const int part = s_part;
     const GridDims& G = J.G;
     const long long ns = G.ns;
     if (*(volatile int*)J.stage == JOB_DONE) continue;  // finished in an earlier launch (all parts agree)
     bool ok = true;
-    PcgState s{};
     // ---------------- set-up: b, C, affine u, energy, z, scalars
     if (*(volatile int*)J.stage == JOB_NEW) {
       double cpart = 0.0;
@@ -338,39 +350,44 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
         const double U0 = C + job_reduce(J, SL_U, red);
         const double gg0 = job_reduce(J, SL_GG, red);
         const double gg = job_reduce(J, SL_ZG, red);
-        s.gg = gg;
-        s.gg0 = (J.criterion == 1) ? gg : gg0;
-        s.rel_res_prev = sqrt(gg / s.gg0);
-        s.rel_res = s.rel_res_prev;
-        s.gamma = 0.0;
-        s.tol = (double)J.tol;
-        s.hAh = 0.0;
-        s.gglast = gg;
-        s.it = 0;
-        s.status = PCG_RUNNING;
-        s.reset = 1;
-        s.resets = 0;
-        s.cur = 0;
-        s.max_iter = J.max_iter;
-        s.divergence_reset = J.divergence_reset;
-        s.refinements = 0;
-        if (part == 0 && threadIdx.x == 0) {
-          J.out->C = C;
-          J.out->utot0 = U0;
-          J.out->gg0 = gg0;
+        if (lead) {
+          s = PcgState{};
+          s.gg = gg;
+          s.gg0 = (J.criterion == 1) ? gg : gg0;
+          s.rel_res_prev = sqrt(gg / s.gg0);
+          s.rel_res = s.rel_res_prev;
+          s.gamma = 0.0;
+          s.tol = (double)J.tol;
+          s.hAh = 0.0;
+          s.gglast = gg;
+          s.it = 0;
+          s.status = PCG_RUNNING;
+          s.reset = 1;
+          s.resets = 0;
+          s.cur = 0;
+          s.max_iter = J.max_iter;
+          s.divergence_reset = J.divergence_reset;
+          s.refinements = 0;
+          s.since_replace = 0;
+          if (part == 0) {
+            J.out->C = C;
+            J.out->utot0 = U0;
+            J.out->gg0 = gg0;
+          }
         }
       }
-    } else {
+    } else if (lead) {
       s = *J.st;  // resume
     }
+    __syncthreads();
     // ---------------- FP32 inner iterations with FP64 residual replacement
     const int R = J.refine_every > 0 ? J.refine_every : 50;
     const int it_end = min(s.it + E.it_limit, s.max_iter);
-    int since = s.since_replace;
     while (ok && s.status == PCG_RUNNING && s.it < it_end) {
       ApplyArgs<float> A = job_apply_args<float>(J);
-      A.x = s.cur ? J.h1 : J.h0;
-      A.hnew = s.cur ? J.h0 : J.h1;
+      const int cur = s.cur;
+      A.x = cur ? J.h1 : J.h0;
+      A.hnew = cur ? J.h0 : J.h1;
       A.zv = J.z32;
       A.y = J.Ah;
       A.gamma = (float)s.gamma;
@@ -380,88 +397,82 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       job_put(J, SL_A, part, hAh_t, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double hAh = job_reduce(J, SL_A, red);
-      s.it += 1;
-      s.cur ^= 1;
-      s.hAh = hAh;
-      if (!isfinite(hAh)) {
-        s.status = PCG_BREAKDOWN;
-        break;
+      if (lead) {
+        s.it += 1;
+        s.cur ^= 1;
+        s.hAh = hAh;
+        if (!isfinite(hAh))
+          s.status = PCG_BREAKDOWN;
+        else if (fabs(hAh) < 1e-14)  // src/elas3dxtal_pcg.f90:1899-1902
+          s.status = PCG_HAH;
       }
-      if (fabs(hAh) < 1e-14) {
-        s.status = PCG_HAH;
-        break;
-      }
+      __syncthreads();
+      if (s.status != PCG_RUNNING) break;
       const float lam = (float)(s.gg / hAh);
-      const float* hc = s.cur ? J.h1 : J.h0;
-      double zg = 0.0;
-      for_part_nodes(J, part, [&](long long m, int, int, int, int tix, int tiy, int tiz, int lx, int ly, int lz) {
-        float ah[3] = {__ldcg(J.Ah + m), __ldcg(J.Ah + m + ns), __ldcg(J.Ah + m + 2 * ns)};
-        halo_add_tile<float>(G, reinterpret_cast<const float*>(J.hx), reinterpret_cast<const float*>(J.hy),
-                             reinterpret_cast<const float*>(J.hd), tix, tiy, tiz, lx, ly, lz, ah);
-        float gv[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const long long i = m + c * ns;
-          J.du[i] = J.du[i] - lam * __ldcg(hc + i);
-          gv[c] = J.g32[i] - lam * ah[c];
-          J.g32[i] = gv[c];
-        }
-        float zv[3];
-        precond3<float>(J.minv32, m, ns, gv, zv);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) J.z32[m + c * ns] = zv[c];
-        zg += (double)(zv[0] * gv[0] + zv[1] * gv[1] + zv[2] * gv[2]);
-      });
+      const double zg = pcg_update_tiles<float>(
+          G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah, reinterpret_cast<const float*>(J.hx),
+          reinterpret_cast<const float*>(J.hy), reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
       job_put(J, SL_B, part, zg, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
-      const double gglast = s.gg;
-      s.gg = job_reduce(J, SL_B, red);
-      s.gglast = gglast;
-      if (!isfinite(s.gg)) {
-        s.status = PCG_BREAKDOWN;
-        break;
+      const double gg_new = job_reduce(J, SL_B, red);
+      if (lead) {
+        const double gglast = s.gg;
+        s.gg = gg_new;
+        s.gglast = gglast;
+        if (!isfinite(gg_new)) {
+          s.status = PCG_BREAKDOWN;
+        } else {
+          const double rel = sqrt(gg_new / s.gg0);
+          s.rel_res = rel;
+          if (s.divergence_reset && rel > 10.0 * s.rel_res_prev && s.it > 1) {  // :1961-1981
+            s.reset = 1;
+            s.resets += 1;
+          } else {
+            s.gamma = gg_new / gglast;
+            s.reset = 0;
+          }
+          s.rel_res_prev = rel;
+          if (rel < s.tol) s.status = PCG_CONVERGED;
+          s.since_replace += 1;
+        }
       }
-      const double rel = sqrt(s.gg / s.gg0);
-      s.rel_res = rel;
-      if (s.divergence_reset && rel > 10.0 * s.rel_res_prev && s.it > 1) {
-        s.reset = 1;
-        s.resets += 1;
-      } else {
-        s.gamma = s.gg / gglast;
-        s.reset = 0;
-      }
-      s.rel_res_prev = rel;
-      if (rel < s.tol) s.status = PCG_CONVERGED;
-      ++since;
-      if (s.status == PCG_CONVERGED || since >= R) {
+      __syncthreads();
+      if (s.status == PCG_BREAKDOWN) break;
+      if (s.status == PCG_CONVERGED || s.since_replace >= R) {
         // FP64 residual replacement: u += du, g = K u + b, restart the FP32 recurrence
         job_fold(J, part);
         if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
         if (!(ok = job_fp64_apply_u(J, part, sm64, E.err, to))) break;
         if (!(ok = job_true_residual(J, part, false, red, E.err, to))) break;
         const double ggt = job_reduce(J, SL_ZG, red);
-        s.gg = ggt;
-        s.refinements += 1;
-        since = 0;
-        if (!isfinite(ggt)) {
-          s.status = PCG_BREAKDOWN;
-          break;
+        if (lead) {
+          s.gg = ggt;
+          s.refinements += 1;
+          s.since_replace = 0;
+          if (!isfinite(ggt)) {
+            s.status = PCG_BREAKDOWN;
+          } else {
+            const double relt = sqrt(ggt / s.gg0);
+            s.rel_res = relt;
+            s.rel_res_prev = relt;
+            if (!s.reset) s.gamma = ggt / s.gglast;
+            s.status = (relt < s.tol) ? PCG_CONVERGED : PCG_RUNNING;
+          }
         }
-        const double relt = sqrt(ggt / s.gg0);
-        s.rel_res = relt;
-        s.rel_res_prev = relt;
-        if (!s.reset) s.gamma = ggt / s.gglast;
-        s.status = (relt < s.tol) ? PCG_CONVERGED : PCG_RUNNING;
+        __syncthreads();
       }
     }
-    if (!ok) s.status = PCG_TIMEOUT;
-    if (ok && s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+    __syncthreads();
+    if (lead) {
+      if (!ok) s.status = PCG_TIMEOUT;
+      if (ok && s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+    }
+    __syncthreads();
     const bool finished = s.status != PCG_RUNNING;
-    s.since_replace = since;
     if (ok && !finished) {
       // out of iteration budget for this launch: persist and yield
-      if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) s.status = PCG_TIMEOUT;
-      if (part == 0 && threadIdx.x == 0) {
+      if (!(ok = job_barrier(J.bar, J.nparts, E.err, to)) && lead) s.status = PCG_TIMEOUT;
+      if (part == 0 && lead) {
         *J.st = s;
         *J.stage = ok ? JOB_ITER : JOB_DONE;
         if (!ok) J.out->status = PCG_TIMEOUT;
@@ -498,7 +509,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       const double gg = job_reduce(J, SL_GG, red);
       double tot[12];
       for (int q = 0; q < 12; ++q) tot[q] = job_reduce(J, SL_S + q, red);
-      if (part == 0 && threadIdx.x == 0) {
+      if (part == 0 && lead) {
         J.out->utot = U;
         J.out->true_rel = sqrt(gg / J.out->gg0);
         for (int r = 0; r < 6; ++r) {
@@ -506,10 +517,10 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
           J.out->epsav[r] = tot[6 + r] / (double)ns;
         }
       }
-    } else {
+    } else if (lead) {
       s.status = PCG_TIMEOUT;
     }
-    if (part == 0 && threadIdx.x == 0) {
+    if (part == 0 && lead) {
       J.out->status = s.status;
       J.out->iterations = s.it;
       J.out->refinements = s.refinements;

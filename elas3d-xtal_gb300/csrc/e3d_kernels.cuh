@@ -1238,6 +1238,77 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
   }
 }
 
+// Phase B of a PCG iteration over tiles first, first + stride, ... < ntiles,
+// node loop in tile order (no index division), z unrolled so several nodes'
+// loads are in flight: u -= lam h, g -= lam Ah (+ tile-edge halos),
+// z = Minv g (src/elas3dxtal_pcg.f90:1913-1932, symmetric Minv); returns this
+// thread's share of z.g (FP32: summed per tile column in FP32, then in FP64).
+template <typename T>
+__device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long first, long long stride, T lam,
+                                                   const T* __restrict__ hc, const T* __restrict__ Ah,
+                                                   const T* __restrict__ hx, const T* __restrict__ hy,
+                                                   const T* __restrict__ hd, const T* __restrict__ minv,
+                                                   T* __restrict__ u, T* __restrict__ g, T* __restrict__ z) {
+  constexpr int U = sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64;
+  const long long ns = G.ns;
+  double zg_t = 0.0;
+  const int tx = threadIdx.x % TILE_X, ty = threadIdx.x / TILE_X;
+  const long long nxy = (long long)G.nx * G.ny;
+  for (long long t = first; t < G.ntiles; t += stride) {
+    const int tix = (int)(t % G.ntx);
+    const int tiy = (int)((t / G.ntx) % G.nty);
+    const int tiz = (int)(t / ((long long)G.ntx * G.nty));
+    const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+    const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+    if (tx >= wx || ty >= wy) continue;
+    const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+    float zg32 = 0.f;  // FP32: this column's z.g, added to the FP64 sum once per tile
+    for (int lz0 = 0; lz0 < wz; lz0 += U) {
+      T ah[U][3], hv[U][3], uv[U][3], gv[U][3], mi[U][6];
+#pragma unroll
+      for (int j = 0; j < U; ++j) {
+        if (lz0 + j < wz) {
+          const long long m = col + nxy * (z0 + lz0 + j);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            ah[j][c] = __ldcg(Ah + m + c * ns);
+            hv[j][c] = __ldcg(hc + m + c * ns);
+            uv[j][c] = u[m + c * ns];
+            gv[j][c] = g[m + c * ns];
+          }
+#pragma unroll
+          for (int q = 0; q < 6; ++q) mi[j][q] = __ldg(minv + m + q * ns);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < U; ++j) {
+        if (lz0 + j < wz) {
+          const long long m = col + nxy * (z0 + lz0 + j);
+          halo_add_tile<T>(G, hx, hy, hd, tix, tiy, tiz, tx, ty, lz0 + j, ah[j]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            u[m + c * ns] = uv[j][c] - lam * hv[j][c];
+            gv[j][c] = gv[j][c] - lam * ah[j][c];
+            g[m + c * ns] = gv[j][c];
+          }
+          const T z0v = mi[j][0] * gv[j][0] + mi[j][3] * gv[j][1] + mi[j][4] * gv[j][2];
+          const T z1v = mi[j][3] * gv[j][0] + mi[j][1] * gv[j][1] + mi[j][5] * gv[j][2];
+          const T z2v = mi[j][4] * gv[j][0] + mi[j][5] * gv[j][1] + mi[j][2] * gv[j][2];
+          z[m] = z0v;
+          z[m + ns] = z1v;
+          z[m + 2 * ns] = z2v;
+          if constexpr (sizeof(T) == 4)
+            zg32 += z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2];
+          else
+            zg_t += (double)(z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2]);
+        }
+      }
+    }
+    if constexpr (sizeof(T) == 4) zg_t += (double)zg32;
+  }
+  return zg_t;
+}
+
 // ---------------------------------------------------------------------------
 // Persistent PCG (dembx_OpenMP main loop, src/elas3dxtal_pcg.f90:1574-2012).
 // One cooperative launch runs up to it_limit iterations; every block keeps an
@@ -1407,65 +1478,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     // ---- phase B: u, g update, preconditioner, z.g -- node loop in tile order
     // (no index division), z unrolled so several nodes' loads are in flight.
     const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
-    double zg_t = 0.0;
-    {
-      constexpr int U = sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64;
-      const int tx = threadIdx.x % TILE_X, ty = threadIdx.x / TILE_X;
-      const long long nxy = (long long)G.nx * G.ny;
-      for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
-        const int tix = (int)(t % G.ntx);
-        const int tiy = (int)((t / G.ntx) % G.nty);
-        const int tiz = (int)(t / ((long long)G.ntx * G.nty));
-        const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
-        const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
-        if (tx >= wx || ty >= wy) continue;
-        const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
-        float zg32 = 0.f;  // FP32: this column's z.g, added to the FP64 sum once per tile
-        for (int lz0 = 0; lz0 < wz; lz0 += U) {
-          T ah[U][3], hv[U][3], uv[U][3], gv[U][3], mi[U][6];
-#pragma unroll
-          for (int j = 0; j < U; ++j) {
-            if (lz0 + j < wz) {
-              const long long m = col + nxy * (z0 + lz0 + j);
-#pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                ah[j][c] = __ldcg(P.Ah + m + c * ns);
-                hv[j][c] = __ldcg(hc + m + c * ns);
-                uv[j][c] = P.u[m + c * ns];
-                gv[j][c] = P.g[m + c * ns];
-              }
-#pragma unroll
-              for (int q = 0; q < 6; ++q) mi[j][q] = __ldg(P.minv + m + q * ns);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < U; ++j) {
-            if (lz0 + j < wz) {
-              const long long m = col + nxy * (z0 + lz0 + j);
-              halo_add_tile<T>(G, P.A.hx, P.A.hy, P.A.hd, tix, tiy, tiz, tx, ty, lz0 + j, ah[j]);
-#pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                P.u[m + c * ns] = uv[j][c] - lam * hv[j][c];
-                gv[j][c] = gv[j][c] - lam * ah[j][c];
-                P.g[m + c * ns] = gv[j][c];
-              }
-              // z = Minv g (src/elas3dxtal_pcg.f90:1930-1932), symmetric Minv
-              const T z0v = mi[j][0] * gv[j][0] + mi[j][3] * gv[j][1] + mi[j][4] * gv[j][2];
-              const T z1v = mi[j][3] * gv[j][0] + mi[j][1] * gv[j][1] + mi[j][5] * gv[j][2];
-              const T z2v = mi[j][4] * gv[j][0] + mi[j][5] * gv[j][1] + mi[j][2] * gv[j][2];
-              P.z[m] = z0v;
-              P.z[m + ns] = z1v;
-              P.z[m + 2 * ns] = z2v;
-              if constexpr (sizeof(T) == 4)
-                zg32 += z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2];
-              else
-                zg_t += (double)(z0v * gv[j][0] + z1v * gv[j][1] + z2v * gv[j][2]);
-            }
-          }
-        }
-        if constexpr (sizeof(T) == 4) zg_t += (double)zg32;
-      }
-    }
+    const double zg_t =
+        pcg_update_tiles<T>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy, P.A.hd, P.minv, P.u, P.g, P.z);
     {
       const double bs = block_sum<NT>(zg_t, red);
       if (threadIdx.x == 0) P.partB[blockIdx.x] = bs;
