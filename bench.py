@@ -413,7 +413,7 @@ def run_form_batch(args):
     nodes = sum(int(np.prod(r["shape"])) for r in rves)
     t0 = time.perf_counter()
     crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
-    b = e3d.Batch(rves, max_iter=20000, criterion=crit)
+    b = e3d.Batch(rves, max_iter=20000, criterion=crit, parts=args.parts)
     t_create = time.perf_counter() - t0
     ceff, sec = b.solve()  # first solve
     ceff, sec = b.solve()  # graph replay (timed)
@@ -549,6 +549,7 @@ def main():
     ap.add_argument("--form", choices=["plain", "solve", "batch", "serve"], default="plain",
                     help="plain: the FP64 DOF-iters/s line; solve/batch/serve: the added forms")
     ap.add_argument("--rves", type=int, default=256, help="batch: ensemble size")
+    ap.add_argument("--parts", type=int, default=0, help="batch: blocks per solve (0: autotune)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=64, help="serve: concurrent solves")

@@ -47,7 +47,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 
 # Every symbol include/e3d_gpu.h and include/e3d_micro.h declare.
 EXPORTED_SYMBOLS = (
-    "e3d_problem_defaults", "e3d_create", "e3d_destroy", "e3d_upload", "e3d_femat",
+    "e3d_problem_defaults", "e3d_create", "e3d_destroy", "e3d_upload", "e3d_upload_device", "e3d_femat",
     "e3d_init_affine", "e3d_energy", "e3d_solve", "e3d_solve_begin", "e3d_iterate",
     "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
@@ -56,6 +56,7 @@ EXPORTED_SYMBOLS = (
     "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
     "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
+    "e3d_micro_grains_device", "e3d_micro_spherical_pores_device", "e3d_micro_ellipsoidal_pores_device",
     "e3d_euler_to_rodrigues",
 )
 
@@ -150,6 +151,13 @@ def load_library(path: str | None = None) -> C.CDLL:
                                             C.c_double, C.c_int32, C.c_uint64, ip]
     L.e3d_micro_ellipsoidal_pores.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
                                               C.c_double, C.c_double, C.c_int32, C.c_uint64, ip]
+    L.e3d_micro_grains_device.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
+                                          C.c_int32, vp, dp]
+    L.e3d_micro_spherical_pores_device.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                                   C.c_double, C.c_int32, C.c_uint64, C.c_int32, vp]
+    L.e3d_micro_ellipsoidal_pores_device.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                                     C.c_double, C.c_double, C.c_int32, C.c_uint64, C.c_int32, vp]
+    L.e3d_upload_device.argtypes = [vp, vp, dp]
     L.e3d_euler_to_rodrigues.argtypes = [C.c_int32, dp, dp]
     L.e3d_euler_to_rodrigues.restype = None
     for name in EXPORTED_SYMBOLS:
@@ -265,6 +273,15 @@ class Elas3D:
         return self._h
 
     # -- inputs (ppixel_hdf5)
+    def upload_device(self, d_pix, rodrigues: np.ndarray | None):
+        """e3d_upload_device: the phase map is already on the device (see micro_grains_device)."""
+        rod = None
+        if rodrigues is not None and self.p.nphase > 1:
+            rod = np.ascontiguousarray(rodrigues, dtype=np.float64).reshape(-1)
+        _check(self.L.e3d_upload_device(self._h, _addr(d_pix), _dp(rod) if rod is not None else None),
+               "e3d_upload_device")
+        return self
+
     def upload(self, pix: np.ndarray, rodrigues: np.ndarray | None):
         pix = np.ascontiguousarray(pix, dtype=np.int32).reshape(-1)
         if pix.size != self.p.ns:
@@ -442,6 +459,44 @@ def micro_ellipsoidal_pores(pix, nx, ny, nz, frac, pore_phase, seed, aspect=4.0,
                                        _ip(pix))
     if rc < 0:
         raise RuntimeError(f"e3d_micro_ellipsoidal_pores failed ({rc})")
+    return rc
+
+
+# GPU versions (same microstructures, bit for bit, in device memory).  d_pix is
+# a device address of nx*ny*nz int32 (an int, or any object with data_ptr(),
+# e.g. a CUDA tensor).
+def _addr(buf):
+    return C.c_void_p(buf.data_ptr() if hasattr(buf, "data_ptr") else int(buf))
+
+
+def micro_grains_device(d_pix, nx, ny, nz, ngrains, seed, laguerre_sigma=0.0, device=0):
+    L = load_library()
+    rod = np.empty(3 * ngrains)
+    rc = L.e3d_micro_grains_device(nx, ny, nz, ngrains, float(laguerre_sigma), int(seed) & (2**64 - 1),
+                                   int(device), _addr(d_pix), _dp(rod))
+    if rc != 0:
+        raise RuntimeError(f"e3d_micro_grains_device failed ({rc}): {L.e3d_last_cuda_error().decode()}")
+    return rod
+
+
+def micro_spherical_pores_device(d_pix, nx, ny, nz, frac, pore_phase, seed, log_mu=np.log(3.0), log_sigma=0.4,
+                                 device=0):
+    L = load_library()
+    rc = L.e3d_micro_spherical_pores_device(nx, ny, nz, float(frac), float(log_mu), float(log_sigma),
+                                            int(pore_phase), int(seed) & (2**64 - 1), int(device), _addr(d_pix))
+    if rc < 0:
+        raise RuntimeError(f"e3d_micro_spherical_pores_device failed ({rc})")
+    return rc
+
+
+def micro_ellipsoidal_pores_device(d_pix, nx, ny, nz, frac, pore_phase, seed, aspect=4.0, log_mu=np.log(2.0),
+                                   log_sigma=0.3, device=0):
+    L = load_library()
+    rc = L.e3d_micro_ellipsoidal_pores_device(nx, ny, nz, float(frac), float(aspect), float(log_mu),
+                                              float(log_sigma), int(pore_phase), int(seed) & (2**64 - 1),
+                                              int(device), _addr(d_pix))
+    if rc < 0:
+        raise RuntimeError(f"e3d_micro_ellipsoidal_pores_device failed ({rc})")
     return rc
 
 

@@ -51,7 +51,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    cu_units = ["e3d_gpu", "e3d_noalloc", "e3d_batch"]
+    cu_units = ["e3d_gpu", "e3d_noalloc", "e3d_batch", "microgen_gpu"]
     cu_objs = [os.path.join(OUT, u + ".o") for u in cu_units]
     cpp_obj = os.path.join(OUT, "microgen.o")
     cu_cmds = []
@@ -61,7 +61,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         if ptxas_info:
             cmd[1:1] = ["-Xptxas", "-v"]
         cu_cmds.append(cmd)
-    cpp_cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I", INCLUDE,
+    cpp_cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-I", INCLUDE,
                "-c", os.path.join(CSRC, "microgen.cpp"), "-o", cpp_obj]
 
     def run(cmd):

@@ -452,6 +452,32 @@ int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
   return E3D_OK;
 }
 
+int32_t e3d_upload_device(e3d_handle_t* h, const int32_t* d_pix, const double* rod) {
+  if (!h || !d_pix) return E3D_ERR_INPUT;
+  const auto& p = h->prob;
+  if (p.flag_m == 1 && p.nphase > 1 && !rod) return E3D_ERR_INPUT;
+  const long long ns = h->G.ns;
+  cudaSetDevice(h->device);
+  E3D_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  pix_from_device_kernel<<<blocks_for(ns, 256), 256, 0, h->stream>>>(ns, d_pix, p.nphase, h->pix, h->err);
+  E3D_LAUNCHED(h);
+  if (rod && p.nphase > 1)
+    E3D_CUDA(cudaMemcpyAsync(h->rod, rod, sizeof(double) * 3 * (p.nphase - 1), cudaMemcpyHostToDevice, h->stream));
+  else
+    E3D_CUDA(cudaMemsetAsync(h->rod, 0, sizeof(double) * 3, h->stream));
+  E3D_CUDA(cudaStreamSynchronize(h->stream));
+  int derr = 0;
+  E3D_CUDA(cudaMemcpy(&derr, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (derr != DEV_OK) {
+    E3D_CUDA(cudaMemset(h->err, 0, sizeof(int)));
+    h->uploaded = false;
+    return E3D_ERR_INPUT;
+  }
+  h->uploaded = true;
+  h->femat_done = h->energy_done = h->solve_ready = h->minv_ready = false;
+  return E3D_OK;
+}
+
 int32_t e3d_femat(e3d_handle_t* h) {
   if (!h) return E3D_ERR_INPUT;
   if (!h->uploaded) return E3D_ERR_STATE;

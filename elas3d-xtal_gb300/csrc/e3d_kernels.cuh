@@ -881,6 +881,21 @@ static __device__ void bond_rotate(const double r[3], double c11, double c12, do
     }
 }
 
+// Phase ids from device memory: 1-based with the range check of ppixel_hdf5
+// (src/elas3dxtal_pcg.f90:2986-2989) -> 0-based; flags DEV_BAD_INDEX.
+static __global__ void pix_from_device_kernel(long long ns, const int32_t* __restrict__ in, int nphase,
+                                              int32_t* __restrict__ out, int* err) {
+  for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (long long)gridDim.x * blockDim.x) {
+    const int32_t v = in[m];
+    if (v < 1 || v > nphase) {
+      atomicExch(err, DEV_BAD_INDEX);
+      out[m] = 0;
+    } else {
+      out[m] = v - 1;
+    }
+  }
+}
+
 // Reference local node r (1..8 -> 0..7) to corner index a = ox + 2oy + 4oz.
 static __constant__ int kRefToCorner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 

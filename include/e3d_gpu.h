@@ -115,6 +115,11 @@ int32_t e3d_destroy(e3d_handle_t* h);
  * 3*(nphase-1) entries (ignored when flag_m == 0, may be NULL then). */
 int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rodrigues);
 
+/* e3d_upload with the phase map already in device memory (d_pix: ns int32 on
+ * the handle's device, e.g. from e3d_micro_grains_device); rodrigues is on the
+ * host.  The range check runs on the device; E3D_ERR_INPUT if it fails. */
+int32_t e3d_upload_device(e3d_handle_t* h, const int32_t* d_pix, const double* rodrigues);
+
 /* femat_OpenMP (:555-1104): cmod (rotatestiffnessby, :2470-2637), element
  * stiffness dk, periodic-jump force b and constant C, all on the device. */
 int32_t e3d_femat(e3d_handle_t* h);

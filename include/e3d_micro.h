@@ -64,6 +64,28 @@ int32_t e3d_micro_read_header(const char* path, int32_t* nx, int32_t* ny,
 int32_t e3d_micro_read(const char* path, int32_t nx, int32_t ny, int32_t nz,
                        int32_t ngrains, int32_t* pix, double* rod);
 
+/* GPU versions of the three generators above: the same microstructures, bit
+ * for bit, written to device memory.  d_pix: nx*ny*nz int32 on CUDA device
+ * `device` (caller-owned; the pore routines read and update it in place);
+ * rod: 3*ngrains doubles on the host.  For the grains the host draws the seeds
+ * and builds the per-block candidate lists and the GPU does the per-voxel
+ * nearest-seed search; the pores are drawn on the host and painted on the GPU
+ * in the host's order.  Temporary device buffers are allocated and freed
+ * inside; calls are synchronous.  Return values as the host routines, and -3
+ * on a CUDA error (text in e3d_last_cuda_error). */
+int32_t e3d_micro_grains_device(int32_t nx, int32_t ny, int32_t nz, int32_t ngrains,
+                                double laguerre_sigma, uint64_t seed, int32_t device,
+                                int32_t* d_pix, double* rod);
+int32_t e3d_micro_spherical_pores_device(int32_t nx, int32_t ny, int32_t nz,
+                                         double target_frac, double log_mu,
+                                         double log_sigma, int32_t pore_phase,
+                                         uint64_t seed, int32_t device, int32_t* d_pix);
+int32_t e3d_micro_ellipsoidal_pores_device(int32_t nx, int32_t ny, int32_t nz,
+                                           double target_frac, double aspect,
+                                           double log_mu, double log_sigma,
+                                           int32_t pore_phase, uint64_t seed,
+                                           int32_t device, int32_t* d_pix);
+
 /* Bunge Euler angles (phi1, Phi, phi2; radians) -> Rodrigues vectors, for
  * callers whose orientation files hold Euler angles.  n orientations. */
 void e3d_euler_to_rodrigues(int32_t n, const double* euler, double* rod);
