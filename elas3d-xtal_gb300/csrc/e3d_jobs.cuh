@@ -276,6 +276,33 @@ static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part
   return job_barrier(J.bar, J.nparts, err, to);
 }
 
+// One FP32 inner iteration's two sweeps, each kept out of line so that it gets
+// its own register allocation rather than the engine kernel's.
+// Fused direction update + stencil: returns this part's h.Ah.
+static __device__ __noinline__ double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
+                                                     ApplySmem<float>& sm) {
+  ApplyArgs<float> A = job_apply_args<float>(J);
+  A.x = cur ? J.h1 : J.h0;
+  A.hnew = cur ? J.h0 : J.h1;
+  A.zv = J.z32;
+  A.y = J.Ah;
+  A.gamma = gamma;
+  A.reset = reset;
+  double hAh = 0.0;
+  for (long long t = part; t < J.G.ntiles; t += J.nparts) {
+    apply_tile<float, true>(A, t, sm, hAh);
+    __syncthreads();
+  }
+  return hAh;
+}
+
+// du -= lam h, g -= lam Ah, z = Minv g: returns this part's z.g.
+static __device__ __noinline__ double job_fp32_update(const JobDesc& J, int part, float lam, int cur) {
+  return pcg_update_tiles<float>(J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah,
+                                 reinterpret_cast<const float*>(J.hx), reinterpret_cast<const float*>(J.hy),
+                                 reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
+}
+
 static __device__ void job_fold(const JobDesc& J, int part) {
   const long long ns = J.G.ns;
   for_part_nodes(J, part, [&](long long m, int, int, int, int, int, int, int, int, int) {
@@ -384,16 +411,8 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
     const int R = J.refine_every > 0 ? J.refine_every : 50;
     const int it_end = min(s.it + E.it_limit, s.max_iter);
     while (ok && s.status == PCG_RUNNING && s.it < it_end) {
-      ApplyArgs<float> A = job_apply_args<float>(J);
       const int cur = s.cur;
-      A.x = cur ? J.h1 : J.h0;
-      A.hnew = cur ? J.h0 : J.h1;
-      A.zv = J.z32;
-      A.y = J.Ah;
-      A.gamma = (float)s.gamma;
-      A.reset = s.reset;
-      double hAh_t = 0.0;
-      job_apply<float, true>(J, part, A, sm32, hAh_t);
+      const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, sm32);
       job_put(J, SL_A, part, hAh_t, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double hAh = job_reduce(J, SL_A, red);
@@ -409,9 +428,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       __syncthreads();
       if (s.status != PCG_RUNNING) break;
       const float lam = (float)(s.gg / hAh);
-      const double zg = pcg_update_tiles<float>(
-          G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah, reinterpret_cast<const float*>(J.hx),
-          reinterpret_cast<const float*>(J.hy), reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
+      const double zg = job_fp32_update(J, part, lam, cur);
       job_put(J, SL_B, part, zg, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double gg_new = job_reduce(J, SL_B, red);
@@ -443,7 +460,9 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
         job_fold(J, part);
         if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
         if (!(ok = job_fp64_apply_u(J, part, sm64, E.err, to))) break;
-        if (!(ok = job_true_residual(J, part, false, red, E.err, to))) break;
+        // energy terms too: if this replacement ends the solve, the final
+        // stage reuses them instead of another FP64 pass over the same u
+        if (!(ok = job_true_residual(J, part, true, red, E.err, to))) break;
         const double ggt = job_reduce(J, SL_ZG, red);
         if (lead) {
           s.gg = ggt;
@@ -457,6 +476,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
             s.rel_res_prev = relt;
             if (!s.reset) s.gamma = ggt / s.gglast;
             s.status = (relt < s.tol) ? PCG_CONVERGED : PCG_RUNNING;
+            s.final_ready = s.status == PCG_CONVERGED;  // u, g and the energy slots are final
           }
         }
         __syncthreads();
@@ -480,12 +500,14 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       continue;
     }
     // ---------------- final: u += du, FP64 energy, true residual, averaged stress
-    if (ok) {
+    // (the first three already done when the solve ended in a replacement)
+    const bool fresh = s.status == PCG_CONVERGED && s.final_ready;
+    if (ok && !fresh) {
       job_fold(J, part);
       ok = job_barrier(J.bar, J.nparts, E.err, to);
     }
-    if (ok) ok = job_fp64_apply_u(J, part, sm64, E.err, to);
-    if (ok) ok = job_true_residual(J, part, true, red, E.err, to);
+    if (ok && !fresh) ok = job_fp64_apply_u(J, part, sm64, E.err, to);
+    if (ok && !fresh) ok = job_true_residual(J, part, true, red, E.err, to);
     double sacc[12];
     for (int q = 0; q < 12; ++q) sacc[q] = 0.0;
     if (ok) {

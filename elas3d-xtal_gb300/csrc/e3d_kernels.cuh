@@ -1336,7 +1336,7 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
 struct PcgState {
   double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
   int it, status, reset, resets, cur, max_iter, divergence_reset, refinements;
-  int since_replace, pad;
+  int since_replace, final_ready;  // final_ready: the job engine ended on a converged FP64 replacement
 };
 
 struct GridBarrier {
@@ -1582,7 +1582,7 @@ static __global__ void pcg_init_scalars_kernel(const double* __restrict__ partia
     S.divergence_reset = divergence_reset;
     S.refinements = 0;
     S.since_replace = 0;
-    S.pad = 0;
+    S.final_ready = 0;
     *st = S;
   }
 }
