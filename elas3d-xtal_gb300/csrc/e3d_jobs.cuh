@@ -149,16 +149,6 @@ __device__ __forceinline__ void for_part_nodes(const JobDesc& J, int part, F&& f
   }
 }
 
-// The heavy steps below are kept out of line so each gets its own register
-// allocation instead of the engine kernel's peak.
-template <typename T, bool FUSED>
-__device__ __noinline__ void job_apply(const JobDesc& J, int part, ApplyArgs<T>& A, ApplySmem<T>& sm, double& hAh) {
-  for (long long t = part; t < J.G.ntiles; t += J.nparts) {
-    apply_tile<T, FUSED>(A, t, sm, hAh);
-    __syncthreads();
-  }
-}
-
 // b at node m: sum over its boundary elements of the row of K_e delta_e.
 static __device__ __noinline__ void job_b_node(const JobDesc& J, int x, int y, int z, double (&acc)[3]) {
   const GridDims& G = J.G;
@@ -231,14 +221,29 @@ inline __device__ ApplyArgs<float> job_apply_args<float>(const JobDesc& J) {
 enum : int { SL_A = 0, SL_B = 1, SL_C = 2, SL_U = 3, SL_GG = 4, SL_ZG = 5, SL_S = 6 /* 6..17 */ };
 constexpr int kJobSlots = 18;
 
-// FP64 K u into g (in-tile part + halos), all parts, then a job barrier.
+// FP64 K u into g (in-tile part + halos), all parts, then a job barrier.  The
+// apply arguments sit in shared memory (read there, not held in registers).
+static __device__ __noinline__ void job_fp64_apply_tiles(const JobDesc& J, int part, ApplySmem<double>& sm) {
+  __shared__ ApplyArgs<double> sA;
+  if (threadIdx.x == 0) {
+    ApplyArgs<double> A = job_apply_args<double>(J);
+    A.x = J.u;
+    A.y = J.g;
+    sA = A;
+  }
+  __syncthreads();
+  double dummy = 0.0;
+  const long long nt = J.G.ntiles;
+  const int np = J.nparts;
+  for (long long t = part; t < nt; t += np) {
+    apply_tile<double, false>(sA, t, sm, dummy);
+    __syncthreads();
+  }
+}
+
 static __device__ bool job_fp64_apply_u(const JobDesc& J, int part, ApplySmem<double>& sm, int* err,
                                  unsigned long long to) {
-  ApplyArgs<double> A = job_apply_args<double>(J);
-  A.x = J.u;
-  A.y = J.g;
-  double dummy = 0.0;
-  job_apply<double, false>(J, part, A, sm, dummy);
+  job_fp64_apply_tiles(J, part, sm);
   return job_barrier(J.bar, J.nparts, err, to);
 }
 
@@ -281,16 +286,23 @@ static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part
 // Fused direction update + stencil: returns this part's h.Ah.
 static __device__ __noinline__ double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
                                                      ApplySmem<float>& sm) {
-  ApplyArgs<float> A = job_apply_args<float>(J);
-  A.x = cur ? J.h1 : J.h0;
-  A.hnew = cur ? J.h0 : J.h1;
-  A.zv = J.z32;
-  A.y = J.Ah;
-  A.gamma = gamma;
-  A.reset = reset;
+  __shared__ ApplyArgs<float> sA;
+  if (threadIdx.x == 0) {
+    ApplyArgs<float> A = job_apply_args<float>(J);
+    A.x = cur ? J.h1 : J.h0;
+    A.hnew = cur ? J.h0 : J.h1;
+    A.zv = J.z32;
+    A.y = J.Ah;
+    A.gamma = gamma;
+    A.reset = reset;
+    sA = A;
+  }
+  __syncthreads();
   double hAh = 0.0;
-  for (long long t = part; t < J.G.ntiles; t += J.nparts) {
-    apply_tile<float, true>(A, t, sm, hAh);
+  const long long nt = J.G.ntiles;
+  const int np = J.nparts;
+  for (long long t = part; t < nt; t += np) {
+    apply_tile<float, true>(sA, t, sm, hAh);
     __syncthreads();
   }
   return hAh;

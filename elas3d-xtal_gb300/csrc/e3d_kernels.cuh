@@ -30,8 +30,19 @@ constexpr int TILE_Y = 8;
 #ifndef E3D_F32_BLOCKS_PER_SM
 #define E3D_F32_BLOCKS_PER_SM 2  // resident 256-thread blocks per SM, FP32 form
 #endif
+// Planes per step of the ring-fed FP32 tile: each thread computes E3D_RING_ZS
+// consecutive elements of its column between two barriers.  ZS = 1 runs two
+// 128-register blocks per SM; ZS = 2 one 255-register block (two independent
+// element computations per thread, no spills) -- measured slower at 500^3
+// (13.3 vs 9.7 ms per inner iteration): occupancy matters more here.
+#ifndef E3D_RING_ZS
+#define E3D_RING_ZS 1
+#endif
 #ifndef E3D_TMA_STAGES
-#define E3D_TMA_STAGES 5  // ring stages per block (two in use, the rest in flight), TMA-fed FP32 stencil
+#define E3D_TMA_STAGES (E3D_RING_ZS + 4)  // ring stages per block (ZS + 1 in use, the rest in flight)
+#endif
+#ifndef E3D_PB_UNROLL_RING
+#define E3D_PB_UNROLL_RING (E3D_RING_ZS == 2 ? 4 : 2)  // phase-B nodes in flight per thread, ring kernel
 #endif
 constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
 
@@ -487,23 +498,28 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   if constexpr (sizeof(T) == 4) hAh += (double)dot32;
 }
 
-// Shared memory of apply_tile_ring: the in-plane force exchange, double-buffered
-// by plane parity so one barrier per plane suffices.
+// Shared memory of apply_tile_ring: the in-plane force exchange of the ZS
+// planes of a step, double-buffered by step parity so one barrier per step
+// suffices.
+template <int ZS>
 struct RingApplySmem {
-  float r[2][9][NT];
+  float r[2][9 * ZS][NT];
 };
 
 // The fused FP32 tile fed by the plane ring (TMA).  Same element arithmetic,
-// values and summation order as apply_tile<float, true> -- the results are
-// bitwise the same -- but every thread reads its element's four corners of
-// plane k+1 straight from the ring stage (main box, or the +x column / +y row /
-// corner box at the tile edge) and forms h_new = z + gamma*h_old there, so no
-// node buffer and no copy barrier are needed; with the force exchange
-// double-buffered one __syncthreads per plane orders the steps, and the oldest
-// stage is refilled right after it.  Plane k uses ring planes R.q (k) and R.q+1
-// (k+1).
-static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile, RingApplySmem& sm, double& hAh,
-                                PlaneRing& R) {
+// values and summation order as apply_tile<float, true>, but every thread reads
+// its element's four corners of the next plane straight from the ring stage
+// (main box, or the +x column / +y row / corner box at the tile edge) and forms
+// h_new = z + gamma*h_old there, so no node buffer and no copy barrier are
+// needed.  A step computes ZS consecutive elements of the thread's column
+// (ZS = 2: two independent element computations between barriers, the shared
+// middle plane transformed once); with the force exchange double-buffered one
+// __syncthreads per step orders the steps, and the step's oldest stages are
+// refilled right after it.  At a step for element planes k .. k+ZS-1 the ring
+// holds plane k at R.q.
+template <int ZS>
+static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile, RingApplySmem<ZS>& sm, double& hAh,
+                                       PlaneRing& R) {
   const GridDims& G = A.g;
   const int tid = threadIdx.x;
   const int tx = tid % TILE_X, ty = tid / TILE_X;
@@ -568,103 +584,117 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
     }
   }
   const int hstride = G.tz;
-  for (int k = z0 - 1; k < z0 + wz; ++k) {
-    const unsigned char* st1 = ring_wait(R, R.q + 1);  // plane k+1
-    float rr[3][4];
-    int ph_nxt = 0;
-    if (active) {
-      float nxt[3][4];
-      corners(st1, nxt);
-      if (k + 1 >= z0 && k + 1 < z0 + wz) {
-        const long long m = ncol + nxy * (k + 1);
+  int step = 0;
+  for (int k = z0 - 1; k < z0 + wz; k += ZS, ++step) {
+    const int ne = min(ZS, z0 + wz - k);  // elements k .. k+ne-1 in this step
+    float rr[ZS][3][4];
+    float hk[ZS][3][4];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = nxt[c][0];
-      }
-      ph_nxt = phase_of(st1);
-      float Pn[3][4], h[3][8];
+    for (int j = 0; j < ZS; ++j) {
+      if (j < ne) {
+        const int kk = k + j;
+        const unsigned char* st1 = ring_wait(R, R.q + 1 + j);  // plane kk+1
+        int ph_nxt = 0;
+        if (active) {
+          float nxt[3][4];
+          corners(st1, nxt);
+          if (kk + 1 >= z0 && kk + 1 < z0 + wz) {
+            const long long m = ncol + nxy * (kk + 1);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        had_xy(nxt[c], Pn[c]);
+            for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = nxt[c][0];
+          }
+          ph_nxt = phase_of(st1);
+          float Pn[3][4], h[3][8];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          h[c][b] = Pn[c][b] + Pold[c][b];
-          h[c][b + 4] = Pn[c][b] - Pold[c][b];
+          for (int c = 0; c < 3; ++c) {
+            had_xy(nxt[c], Pn[c]);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              h[c][b] = Pn[c][b] + Pold[c][b];
+              h[c][b + 4] = Pn[c][b] - Pold[c][b];
+            }
+          }
+          float f[3][8];
+          element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float lo[4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              lo[b] = f[c][b] - f[c][b + 4];
+              const float hi = f[c][b] + f[c][b + 4];
+              if (kk >= z0) lo[b] += carry[c][b];
+              carry[c][b] = hi;
+            }
+            if (kk >= z0) had_xy_adj(lo, rr[j][c]);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+          }
         }
-      }
-      float f[3][8];
-      element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+        // plane kk's h_new for the dot products, read before the barrier (the
+        // stage is refilled after it)
+        if (kk >= z0 && active) {
+          const unsigned char* st0 = ring_stage(R, R.q + j);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float lo[4];
+          for (int d = 0; d < 4; ++d) {
+            const bool need = d == 0 || (d == 1 && tx == wx - 1) || (d == 2 && ty == wy - 1) ||
+                              (d == 3 && tx == wx - 1 && ty == wy - 1);
+            int off, str;
+            corner_at(d, off, str);
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          lo[b] = f[c][b] - f[c][b + 4];
-          const float hi = f[c][b] + f[c][b + 4];
-          if (k >= z0) lo[b] += carry[c][b];
-          carry[c][b] = hi;
+            for (int c = 0; c < 3; ++c) hk[j][c][d] = need ? hval(st0, off + c * str) : 0.f;
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            sm.r[step & 1][9 * j + 3 * c + 0][tid] = rr[j][c][1];  // to node (x+1, y)
+            sm.r[step & 1][9 * j + 3 * c + 1][tid] = rr[j][c][2];  // to node (x, y+1)
+            sm.r[step & 1][9 * j + 3 * c + 2][tid] = rr[j][c][3];  // to node (x+1, y+1)
+          }
         }
-        if (k >= z0) had_xy_adj(lo, rr[c]);
-#pragma unroll
-        for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
-      }
-    }
-    // plane k's h_new for the dot products, read before the barrier (the
-    // stage is refilled after it)
-    float hk[3][4];
-    if (k >= z0 && active) {
-      const unsigned char* st0 = ring_stage(R, R.q);
-#pragma unroll
-      for (int d = 0; d < 4; ++d) {
-        const bool need = d == 0 || (d == 1 && tx == wx - 1) || (d == 2 && ty == wy - 1) ||
-                          (d == 3 && tx == wx - 1 && ty == wy - 1);
-        int off, str;
-        corner_at(d, off, str);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) hk[c][d] = need ? hval(st0, off + c * str) : 0.f;
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        sm.r[k & 1][3 * c + 0][tid] = rr[c][1];  // to node (x+1, y)
-        sm.r[k & 1][3 * c + 1][tid] = rr[c][2];  // to node (x, y+1)
-        sm.r[k & 1][3 * c + 2][tid] = rr[c][3];  // to node (x+1, y+1)
+        ph_cur = ph_nxt;
       }
     }
     __syncthreads();
-    ring_release(R, G);  // plane k
-    if (k >= z0 && active) {
-      const float(*r)[NT] = sm.r[k & 1];
-      const int lz = k - z0;
-      const long long m = ncol + nxy * k;
-      float hxv[3], hyv[3], acc[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        acc[c] = rr[c][0];
-        if (tx > 0) acc[c] += r[3 * c + 0][tid - 1];
-        if (ty > 0) acc[c] += r[3 * c + 1][tid - TILE_X];
-        if (tx > 0 && ty > 0) acc[c] += r[3 * c + 2][tid - TILE_X - 1];
-        A.y[m + c * ns] = acc[c];
-        hxv[c] = rr[c][1] + (ty > 0 ? r[3 * c + 2][tid - TILE_X] : 0.f);
-        hyv[c] = rr[c][2] + (tx > 0 ? r[3 * c + 2][tid - 1] : 0.f);
-      }
-      dot32 += hk[0][0] * acc[0] + hk[1][0] * acc[1] + hk[2][0] * acc[2];
-      const long long hb = tile * hstride + lz;
-      if (tx == wx - 1) {
+    for (int j = 0; j < ZS; ++j)
+      if (j < ne) ring_release(R, G);  // planes k .. k+ne-1
 #pragma unroll
-        for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * hstride + hb) * TILE_Y + ty] = hxv[c];
-        dot32 += hk[0][1] * hxv[0] + hk[1][1] * hxv[1] + hk[2][1] * hxv[2];
-      }
-      if (ty == wy - 1) {
+    for (int j = 0; j < ZS; ++j) {
+      const int kk = k + j;
+      if (j < ne && kk >= z0 && active) {
+        const float(*r)[NT] = sm.r[step & 1] + 9 * j;
+        const int lz = kk - z0;
+        const long long m = ncol + nxy * kk;
+        float hxv[3], hyv[3], acc[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * hstride + hb) * TILE_X + tx] = hyv[c];
-        dot32 += hk[0][2] * hyv[0] + hk[1][2] * hyv[1] + hk[2][2] * hyv[2];
-      }
-      if (tx == wx - 1 && ty == wy - 1) {
+        for (int c = 0; c < 3; ++c) {
+          acc[c] = rr[j][c][0];
+          if (tx > 0) acc[c] += r[3 * c + 0][tid - 1];
+          if (ty > 0) acc[c] += r[3 * c + 1][tid - TILE_X];
+          if (tx > 0 && ty > 0) acc[c] += r[3 * c + 2][tid - TILE_X - 1];
+          A.y[m + c * ns] = acc[c];
+          hxv[c] = rr[j][c][1] + (ty > 0 ? r[3 * c + 2][tid - TILE_X] : 0.f);
+          hyv[c] = rr[j][c][2] + (tx > 0 ? r[3 * c + 2][tid - 1] : 0.f);
+        }
+        dot32 += hk[j][0][0] * acc[0] + hk[j][1][0] * acc[1] + hk[j][2][0] * acc[2];
+        const long long hb = tile * hstride + lz;
+        if (tx == wx - 1) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * hstride + hb] = rr[c][3];
-        dot32 += hk[0][3] * rr[0][3] + hk[1][3] * rr[1][3] + hk[2][3] * rr[2][3];
+          for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * hstride + hb) * TILE_Y + ty] = hxv[c];
+          dot32 += hk[j][0][1] * hxv[0] + hk[j][1][1] * hxv[1] + hk[j][2][1] * hxv[2];
+        }
+        if (ty == wy - 1) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * hstride + hb) * TILE_X + tx] = hyv[c];
+          dot32 += hk[j][0][2] * hyv[0] + hk[j][1][2] * hyv[1] + hk[j][2][2] * hyv[2];
+        }
+        if (tx == wx - 1 && ty == wy - 1) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * hstride + hb] = rr[j][c][3];
+          dot32 += hk[j][0][3] * rr[j][0][3] + hk[j][1][3] * rr[j][1][3] + hk[j][2][3] * rr[j][2][3];
+        }
       }
     }
-    ph_cur = ph_nxt;
   }
   ring_release(R, G);  // plane z0+wz, last read before the final step's barrier
   hAh += (double)dot32;
@@ -1258,13 +1288,12 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
 // loads are in flight: u -= lam h, g -= lam Ah (+ tile-edge halos),
 // z = Minv g (src/elas3dxtal_pcg.f90:1913-1932, symmetric Minv); returns this
 // thread's share of z.g (FP32: summed per tile column in FP32, then in FP64).
-template <typename T>
+template <typename T, int U = (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64)>
 __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long first, long long stride, T lam,
                                                    const T* __restrict__ hc, const T* __restrict__ Ah,
                                                    const T* __restrict__ hx, const T* __restrict__ hy,
                                                    const T* __restrict__ hd, const T* __restrict__ minv,
                                                    T* __restrict__ u, T* __restrict__ g, T* __restrict__ z) {
-  constexpr int U = sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64;
   const long long ns = G.ns;
   double zg_t = 0.0;
   const int tx = threadIdx.x % TILE_X, ty = threadIdx.x / TILE_X;
@@ -1424,9 +1453,10 @@ struct PcgArgs {
 // TMA (FP32 only): phase A reads its node planes through the block's plane
 // ring (dynamic shared memory of kRingSmemBytes).
 template <typename T, bool TMA = false>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1) pcg_persistent_kernel(PcgArgs<T> P) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 ? 1 : E3D_F32_BLOCKS_PER_SM) : 1)
+    pcg_persistent_kernel(PcgArgs<T> P) {
   static_assert(!TMA || sizeof(T) == 4, "the plane ring feeds the FP32 stencil");
-  using Smem = std::conditional_t<TMA, RingApplySmem, ApplySmem<T>>;
+  using Smem = std::conditional_t<TMA, RingApplySmem<E3D_RING_ZS>, ApplySmem<T>>;
   __shared__ Smem sm;
   __shared__ double red[NT / 32];
   __shared__ PcgState S0;
@@ -1462,7 +1492,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     if constexpr (TMA) ring_begin(ring, G, cur ? P.maps->h1 : P.maps->h0, blockIdx.x, gridDim.x, G.ntiles);
     for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
       if constexpr (TMA)
-        apply_tile_ring(A, t, sm, hAh_t, ring);
+        apply_tile_ring<E3D_RING_ZS>(A, t, sm, hAh_t, ring);
       else
         apply_tile<T, true>(A, t, sm, hAh_t);
       __syncthreads();
@@ -1493,8 +1523,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? E3D_F32_BLOCKS_PER_SM : 1
     // ---- phase B: u, g update, preconditioner, z.g -- node loop in tile order
     // (no index division), z unrolled so several nodes' loads are in flight.
     const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
-    const double zg_t =
-        pcg_update_tiles<T>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy, P.A.hd, P.minv, P.u, P.g, P.z);
+    constexpr int U = TMA ? E3D_PB_UNROLL_RING : (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64);
+    const double zg_t = pcg_update_tiles<T, U>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy, P.A.hd,
+                                               P.minv, P.u, P.g, P.z);
     {
       const double bs = block_sum<NT>(zg_t, red);
       if (threadIdx.x == 0) P.partB[blockIdx.x] = bs;

@@ -2,9 +2,12 @@
 cp.async.bulk.tensor through an mbarrier ring) against the FP32 stencil with
 per-thread loads and against the FP64 oracle.
 
-Both FP32 paths do the same arithmetic on the same values in the same order and
-launch the same number of blocks, so their solves are bitwise identical.
-Against the oracle the mixed-form bar holds: energy within 1e-8."""
+Both FP32 paths do the same per-node arithmetic on the same values in the same
+order; they may launch different numbers of blocks (the ring kernel runs one
+255-register block per SM), which regroups the FP64 block partial sums of the
+dot products, so their solves agree to rounding: iteration counts within 1,
+energies within 1e-11 relative, displacements within 1e-7.  Against the oracle
+the mixed-form bar holds: energy within 1e-8."""
 import numpy as np
 import pytest
 
@@ -66,9 +69,9 @@ def test_tma_stencil_matches_per_thread_loads(shape, monkeypatch):
     path_r, rr, ur = _solve(p, pix, rod, True, monkeypatch)
     assert path_t == "f32_tma" and path_r == "f32"
     assert rt["exit_reason"] == e3d.EXIT_CONVERGED and rr["exit_reason"] == e3d.EXIT_CONVERGED
-    assert rt["iterations"] == rr["iterations"]
-    assert rt["utot"] == rr["utot"]
-    assert np.array_equal(ut, ur)
+    assert abs(rt["iterations"] - rr["iterations"]) <= 1
+    assert abs(rt["utot"] - rr["utot"]) <= 1e-11 * abs(rr["utot"])
+    assert _rel(ut, ur) < 1e-7
     ref = O.run(_oracle_problem(p), pix, rod)
     assert abs(rt["utot"] - ref["utot"]) <= 1e-8 * abs(ref["utot"])
 
