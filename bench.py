@@ -422,6 +422,7 @@ def run_form_batch(args):
     b.close()
     nj = len(res)
     iters = [r["iterations"] for r in res]
+    node_iters = float(sum(int(np.prod(rves[r["rve"]]["shape"])) * r["iterations"] for r in res))
     conv = sum(r["status"] == e3d.EXIT_CONVERGED for r in res)
     # reference: plain sequential FP64 GPU solves of a seeded sample of the same jobs
     rng = np.random.default_rng(0)
@@ -444,6 +445,7 @@ def run_form_batch(args):
                                                            "mean": float(np.mean(iters))},
             "parts_hist": {str(k): int((parts == k).sum()) for k in sorted(set(parts.tolist()))},
             "create_seconds": t_create, "rve_nodes": nodes,
+            "work": {"node_iterations": node_iters, "dof_iters_per_s": 3.0 * node_iters / sec},
             "sequential_fp64": {"solves_per_s": seq_rate, "sample": len(seq),
                                 "sample_seconds": sum(seq),
                                 "energy_rel_err_vs_batched": {"max": max(errs), "median": float(np.median(errs))}},
@@ -503,6 +505,7 @@ def run_form_serve(args):
     srv.close()
     lat = np.array([done_at[rid] - arrivals[k] for k, rid in enumerate(ids)])
     conv = sum(r["status"] == e3d.EXIT_CONVERGED for r in res)
+    node_iters = float(sum(int(np.prod(rv["shape"])) * r["iterations"] for (rv, _), r in zip(reqs, res)))
     # reference: the same requests as plain sequential FP64 GPU solves (sample)
     m = min(args.sample, len(reqs))
     seq, errs = [], []
@@ -524,6 +527,10 @@ def run_form_serve(args):
                                                                    "max": float(lat.max())},
             "peak_hbm_bytes": peak, "hbm_budget": budget, "slots": args.slots, "round_iters": args.round_iters,
             "criterion": args.criterion,
+            "work": {"node_iterations": node_iters, "dof_iters_per_s": 3.0 * node_iters / total,
+                     "iterations": {"min": int(min(r["iterations"] for r in res)),
+                                    "max": int(max(r["iterations"] for r in res)),
+                                    "mean": float(np.mean([r["iterations"] for r in res]))}},
             "sequential_fp64": {"sample": m, "solves_per_s": m / sum(seq),
                                 "energy_rel_err_vs_served": {"max": max(errs), "median": float(np.median(errs))},
                                 "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
