@@ -59,9 +59,31 @@ struct GridDims {
   long long ntiles;
 };
 
+// Periodic wrap of v into [0, n); the callers pass neighbours (v in [-n, 2n)),
+// handled without an integer division.
 __host__ __device__ inline int wrapi(int v, int n) {
+  if (v >= 0 && v < n) return v;
+  if (v < 0 && v >= -n) return v + n;
+  if (v >= n && v < 2 * n) return v - n;
   v %= n;
   return v < 0 ? v + n : v;
+}
+
+// Node index -> (x, y, z); 32-bit division when the grid allows it (every grid
+// up to 2^32 nodes), far cheaper than the 64-bit one.
+__device__ __forceinline__ void node_xyz(const GridDims& G, long long m, int& x, int& y, int& z) {
+  if (G.ns <= 0xffffffffLL) {
+    const unsigned mm = (unsigned)m, nx = (unsigned)G.nx, ny = (unsigned)G.ny;
+    const unsigned q = mm / nx;
+    x = (int)(mm - q * nx);
+    const unsigned r = q / ny;
+    y = (int)(q - r * ny);
+    z = (int)r;
+  } else {
+    x = (int)(m % G.nx);
+    y = (int)((m / G.nx) % G.ny);
+    z = (int)(m / ((long long)G.nx * G.ny));
+  }
 }
 
 template <typename T>
@@ -776,9 +798,8 @@ __global__ void apply_finish_kernel(GridDims G, const T* __restrict__ yin, const
                                     T* __restrict__ yout) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
-  const int x = (int)(m % G.nx);
-  const int y = (int)((m / G.nx) % G.ny);
-  const int z = (int)(m / ((long long)G.nx * G.ny));
+  int x, y, z;
+  node_xyz(G, m, x, y, z);
   T v[3] = {yin[m], yin[m + G.ns], yin[m + 2 * G.ns]};
   halo_add<T>(G, hx, hy, hd, x, y, z, v);
   yout[m] = v[0];
@@ -799,9 +820,8 @@ static __global__ void __launch_bounds__(256) energy_finish_kernel(GridDims G, c
   double eu = 0.0, gg = 0.0;
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
        m += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(m % G.nx);
-    const int y = (int)((m / G.nx) % G.ny);
-    const int z = (int)(m / ((long long)G.nx * G.ny));
+    int x, y, z;
+    node_xyz(G, m, x, y, z);
     double v[3] = {ku[m], ku[m + G.ns], ku[m + 2 * G.ns]};
     halo_add<double>(G, hx, hy, hd, x, y, z, v);
 #pragma unroll
@@ -1020,9 +1040,8 @@ static __global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* _
                                const double* __restrict__ dk, double* __restrict__ b) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
-  const int x = (int)(m % G.nx);
-  const int y = (int)((m / G.nx) % G.ny);
-  const int z = (int)(m / ((long long)G.nx * G.ny));
+  int x, y, z;
+  node_xyz(G, m, x, y, z);
   double acc[3] = {0.0, 0.0, 0.0};
   const bool edge = (x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1);
   if (edge) {
@@ -1099,9 +1118,9 @@ static __global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpPar
 static __global__ void affine_kernel(GridDims G, JumpParams J, double* __restrict__ u) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
-  const double x = (double)(m % G.nx);
-  const double y = (double)((m / G.nx) % G.ny);
-  const double z = (double)(m / ((long long)G.nx * G.ny));
+  int xi, yi, zi;
+  node_xyz(G, m, xi, yi, zi);
+  const double x = xi, y = yi, z = zi;
   const double exx = J.E[0][0], eyy = J.E[1][1], ezz = J.E[2][2];
   const double exy = J.E[0][1], exz = J.E[0][2], eyz = J.E[1][2];
   u[m] = x * exx + y * exy + z * exz;
@@ -1153,9 +1172,8 @@ static __global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pi
     }
     return;
   }
-  const int x = (int)(m % G.nx);
-  const int y = (int)((m / G.nx) % G.ny);
-  const int z = (int)(m / ((long long)G.nx * G.ny));
+  int x, y, z;
+  node_xyz(G, m, x, y, z);
   double M[3][3];
   for (int ra = 0; ra < 8; ++ra) {
     const int a = kRefToCorner[ra];
@@ -1240,9 +1258,8 @@ static __global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, Jump
   for (int t = 0; t < 12; ++t) acc[t] = 0.0;
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
        m += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(m % G.nx);
-    const int y = (int)((m / G.nx) % G.ny);
-    const int z = (int)(m / ((long long)G.nx * G.ny));
+    int x, y, z;
+    node_xyz(G, m, x, y, z);
     double eps[6];
     voxel_strain(G, J, u, x, y, z, eps);
     const int ph = pix[m];
@@ -1264,9 +1281,8 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
                                     double* __restrict__ sigma, double* __restrict__ vm) {
   const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= G.ns) return;
-  const int x = (int)(m % G.nx);
-  const int y = (int)((m / G.nx) % G.ny);
-  const int z = (int)(m / ((long long)G.nx * G.ny));
+  int x, y, z;
+  node_xyz(G, m, x, y, z);
   double eps[6];
   voxel_strain(G, J, u, x, y, z, eps);
   const int ph = pix[m];
@@ -1642,9 +1658,8 @@ static __global__ void __launch_bounds__(256) true_residual_kernel(GridDims G, c
   double acc = 0.0;
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < G.ns;
        m += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(m % G.nx);
-    const int y = (int)((m / G.nx) % G.ny);
-    const int z = (int)(m / ((long long)G.nx * G.ny));
+    int x, y, z;
+    node_xyz(G, m, x, y, z);
     double v[3] = {ku[m], ku[m + G.ns], ku[m + 2 * G.ns]};
     halo_add<double>(G, hx, hy, hd, x, y, z, v);
     float gv[3];
