@@ -447,6 +447,8 @@ def run_form_batch(args):
             "solves": nj, "converged": conv, "iterations": {"min": min(iters), "max": max(iters),
                                                            "mean": float(np.mean(iters))},
             "parts_hist": {str(k): int((parts == k).sum()) for k in sorted(set(parts.tolist()))},
+            "tile_z_hist": {str(t): sum(1 for r in res if r["tile_z"] == t)
+                            for t in sorted(set(r["tile_z"] for r in res))},
             "create_seconds": t_create, "rve_nodes": nodes,
             "work": {"node_iterations": node_iters, "dof_iters_per_s": 3.0 * node_iters / sec},
             "sequential_fp64": {"solves_per_s": seq_rate, "sample": len(seq),

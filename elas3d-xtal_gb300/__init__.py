@@ -559,12 +559,12 @@ class BatchOptsC(C.Structure):
 class JobResultC(C.Structure):
     _fields_ = [("rve", C.c_int32), ("load_case", C.c_int32), ("status", C.c_int32),
                 ("iterations", C.c_int32), ("refinements", C.c_int32), ("resets", C.c_int32),
-                ("parts", C.c_int32), ("pad", C.c_int32), ("utot0", C.c_double), ("utot", C.c_double),
+                ("parts", C.c_int32), ("tile_z", C.c_int32), ("utot0", C.c_double), ("utot", C.c_double),
                 ("rel_res", C.c_double), ("true_rel", C.c_double), ("strav", C.c_double * 6),
                 ("epsav", C.c_double * 6), ("seconds", C.c_double)]
 
     def as_dict(self) -> dict:
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("strav", "epsav", "pad")}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("strav", "epsav")}
         d["strav"] = np.array(self.strav[:])
         d["epsav"] = np.array(self.epsav[:])
         return d

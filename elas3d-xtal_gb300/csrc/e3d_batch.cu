@@ -34,13 +34,17 @@ namespace {
 
 constexpr int kPartChoices[] = {1, 2, 4, 8, 16, 32, 64};
 constexpr int kMaxParts = 64;
+// Tile depths along z the autotuner tries (0: the rule of job_dims).
+constexpr int kTzChoices[] = {0, 16, 32};
 constexpr unsigned long long kTimeoutNs = 120ull * 1000000000ull;
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Tiles of one solve run by k parts: split z so that there are at least ~4
-// tiles per part, but keep z chunks of >= 16 planes (one redundant plane each).
-GridDims job_dims(int nx, int ny, int nz, int k) {
+// Tiles of one solve run by k parts.  tz_req > 0: z chunks of that many planes
+// (the tile shape the autotuner picked); otherwise split z so that there are at
+// least ~4 tiles per part, keeping chunks of >= 16 planes (one redundant
+// element plane each).
+GridDims job_dims(int nx, int ny, int nz, int k, int tz_req = 0) {
   GridDims G{};
   G.nx = nx;
   G.ny = ny;
@@ -53,6 +57,7 @@ GridDims job_dims(int nx, int ny, int nz, int k) {
   int ntz = (int)std::max<long long>(1, std::min<long long>(nz, (want + cols - 1) / cols));
   int tz = (nz + ntz - 1) / ntz;
   if (tz < 16) tz = std::min(nz, 16);
+  if (tz_req > 0) tz = std::min(nz, tz_req);
   G.tz = tz;
   G.ntz = (nz + tz - 1) / tz;
   G.ntiles = cols * G.ntz;
@@ -63,7 +68,8 @@ long long halo_doubles(const GridDims& G) { return 3LL * G.ntiles * G.tz * (TILE
 
 long long max_halo_doubles(int nx, int ny, int nz) {
   long long m = 0;
-  for (int k = 1; k <= kMaxParts; ++k) m = std::max(m, halo_doubles(job_dims(nx, ny, nz, k)));
+  for (int k = 1; k <= kMaxParts; ++k)
+    for (int tz : kTzChoices) m = std::max(m, halo_doubles(job_dims(nx, ny, nz, k, tz)));
   return m;
 }
 
@@ -216,9 +222,9 @@ void fill_job(JobDev& J, const RveDev& R, char*& p, const double strain[6], int 
   d.tol = tol;
 }
 
-void set_parts(JobDev& J, const RveDev& R, int k) {
+void set_parts(JobDev& J, const RveDev& R, int k, int tz_req = 0) {
   JobDesc& d = J.d;
-  d.G = job_dims(R.nx, R.ny, R.nz, k);
+  d.G = job_dims(R.nx, R.ny, R.nz, k, tz_req);
   d.nparts = k;
   const long long h = (long long)d.G.ntiles * d.G.tz;
   double* base = d.hx;
@@ -336,9 +342,9 @@ struct e3d_batch {
 
 namespace {
 
-int32_t batch_time_job(e3d_batch* b, size_t j, int k, int iters, float* ms) {
+int32_t batch_time_job(e3d_batch* b, size_t j, int k, int tz_req, int iters, float* ms) {
   JobDev J = b->jobs[j];
-  set_parts(J, b->rves[(size_t)J.rve], k);
+  set_parts(J, b->rves[(size_t)J.rve], k, tz_req);
   std::vector<JobDesc> one{J.d};
   int np = 0;
   int32_t rc = b->eng.upload(one, b->stream, &np);
@@ -359,18 +365,20 @@ int32_t batch_time_job(e3d_batch* b, size_t j, int k, int iters, float* ms) {
 }
 
 // Autotuner: per size class (node count within a factor of two), time the
-// engine on one representative solve for each candidate k (set-up + 2
-// iterations vs set-up + 10), then choose k per class to minimise the
-// estimated makespan max(total block-time / resident blocks, longest solve).
-int32_t batch_autotune(e3d_batch* b, std::vector<int>& kjob) {
+// engine on one representative solve for each candidate schedule -- blocks per
+// solve k and tile shape (element planes per tile, kTzChoices) -- as set-up + 10
+// iterations minus set-up + 2; keep the fastest tile shape per k, then choose k
+// per class to minimise the estimated makespan max(total block-time / resident
+// blocks, longest solve).
+int32_t batch_autotune(e3d_batch* b, std::vector<int>& kjob, std::vector<int>& tzjob) {
   std::map<int, std::vector<size_t>> cls;  // log2(ns) -> solves
   for (size_t j = 0; j < b->jobs.size(); ++j) {
     const long long ns = b->rves[(size_t)b->jobs[j].rve].ns;
     cls[(int)std::floor(std::log2((double)ns))].push_back(j);
   }
   struct C {
-    std::vector<int> ks;
-    std::vector<double> t;  // ms per iteration per solve
+    std::vector<int> ks, tzs;  // per k: the fastest tile depth
+    std::vector<double> t;     // ms per iteration per solve
     int pick = 0;
     size_t n = 0;
   };
@@ -383,12 +391,24 @@ int32_t batch_autotune(e3d_batch* b, std::vector<int>& kjob) {
     for (int k : kPartChoices) {
       const GridDims G = job_dims(R.nx, R.ny, R.nz, k);
       if (k > 1 && G.ntiles < 2LL * k) break;  // too few tiles to share
-      float t2 = 0.f, t10 = 0.f;
-      int32_t rc = batch_time_job(b, rep, k, 2, &t2);
-      if (!rc) rc = batch_time_job(b, rep, k, 10, &t10);
-      if (rc) return rc;
+      double best_t = 1e300;
+      int best_tz = 0;
+      for (int tz : kTzChoices) {
+        const GridDims Gt = job_dims(R.nx, R.ny, R.nz, k, tz);
+        if (tz > 0 && (Gt.tz == G.tz || Gt.ntiles < (long long)k)) continue;  // same shape, or too few tiles
+        float t2 = 0.f, t10 = 0.f;
+        int32_t rc = batch_time_job(b, rep, k, tz, 2, &t2);
+        if (!rc) rc = batch_time_job(b, rep, k, tz, 10, &t10);
+        if (rc) return rc;
+        const double t = std::max(1e-6, (double)(t10 - t2) / 8.0);
+        if (t < best_t) {
+          best_t = t;
+          best_tz = tz;
+        }
+      }
       c.ks.push_back(k);
-      c.t.push_back(std::max(1e-6, (double)(t10 - t2) / 8.0));
+      c.tzs.push_back(best_tz);
+      c.t.push_back(best_t);
     }
     // start from the most block-efficient choice
     size_t best = 0;
@@ -414,8 +434,13 @@ int32_t batch_autotune(e3d_batch* b, std::vector<int>& kjob) {
     c.pick += 1;  // split the longest solves over more blocks
   }
   kjob.assign(b->jobs.size(), 1);
+  tzjob.assign(b->jobs.size(), 0);
   for (auto& kv : cls)
-    for (size_t j : kv.second) kjob[j] = cc[kv.first].ks[(size_t)cc[kv.first].pick];
+    for (size_t j : kv.second) {
+      const C& c = cc[kv.first];
+      kjob[j] = c.ks[(size_t)c.pick];
+      tzjob[j] = c.tzs[(size_t)c.pick];
+    }
   return E3D_OK;
 }
 
@@ -517,14 +542,14 @@ int32_t e3d_batch_create(e3d_batch_t** out, const e3d_rve_t* rves, int32_t n, co
     b->order.push_back(J.rve * (int)cases.size() + ci);
   }
   // blocks per solve
-  std::vector<int> kjob(b->jobs.size(), 1);
+  std::vector<int> kjob(b->jobs.size(), 1), tzjob(b->jobs.size(), 0);
   if (o->parts > 0) {
     for (size_t j = 0; j < b->jobs.size(); ++j) kjob[j] = std::min(o->parts, kMaxParts);
-  } else if ((rc = batch_autotune(b, kjob))) {
+  } else if ((rc = batch_autotune(b, kjob, tzjob))) {
     return fail(rc);
   }
   for (size_t j = 0; j < b->jobs.size(); ++j) {
-    set_parts(b->jobs[j], b->rves[(size_t)b->jobs[j].rve], std::min(kjob[j], b->eng.grid));
+    set_parts(b->jobs[j], b->rves[(size_t)b->jobs[j].rve], std::min(kjob[j], b->eng.grid), tzjob[j]);
     b->descs.push_back(b->jobs[j].d);
   }
   if ((rc = b->eng.upload(b->descs, b->stream, &b->nparts_total))) return fail(rc);
@@ -601,6 +626,7 @@ int32_t e3d_batch_results(e3d_batch_t* b, e3d_job_result_t* out, int32_t capacit
     o.refinements = r.refinements;
     o.resets = r.resets;
     o.parts = b->jobs[(size_t)j].d.nparts;
+    o.tile_z = b->jobs[(size_t)j].d.G.tz;
     o.utot0 = r.utot0;
     o.utot = r.utot;
     o.rel_res = r.rel_res;
@@ -795,6 +821,7 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
       o.refinements = r.refinements;
       o.resets = r.resets;
       o.parts = j->J.d.nparts;
+      o.tile_z = j->J.d.G.tz;
       o.utot0 = r.utot0;
       o.utot = r.utot;
       o.rel_res = r.rel_res;

@@ -53,7 +53,8 @@ typedef struct e3d_job_result {
   int32_t rve, load_case;   /* load_case 0..5 (xx yy zz xz yz xy), -1 for served requests */
   int32_t status;           /* E3D_EXIT_* of e3d_gpu.h                           */
   int32_t iterations, refinements, resets;
-  int32_t parts, pad;
+  int32_t parts;             /* blocks that ran the solve                         */
+  int32_t tile_z;            /* element planes per tile (autotuned tile shape)    */
   double utot0, utot;       /* initial / final energy                            */
   double rel_res, true_rel; /* criterion value and |g|/|g0| at exit              */
   double strav[6], epsav[6];
@@ -66,7 +67,7 @@ void e3d_batch_opts_defaults(e3d_batch_opts_t* o);
 
 /* Uploads the RVEs, builds every phase table (femat element part) and
  * block-Jacobi inverse, allocates all solve state (within hbm_budget), picks
- * the blocks per solve (autotuner when opts->parts == 0) and captures the
+ * the blocks per solve and the tile shape (autotuner when opts->parts == 0) and captures the
  * solve into a CUDA graph. */
 int32_t e3d_batch_create(e3d_batch_t** b, const e3d_rve_t* rves, int32_t n, const e3d_batch_opts_t* opts);
 

@@ -38,6 +38,8 @@ def test_batch_matches_oracle(small_ensemble):
         parts = b.parts()
     assert sec > 0 and set(parts.tolist()) <= {1, 2, 4, 8, 16}
     assert len(res) == 6 * len(rves)
+    # the autotuned tile shape: element planes per tile within the RVE's depth
+    assert all(1 <= r["tile_z"] <= rves[r["rve"]]["shape"][2] for r in res)
     for r in res:
         assert r["status"] == e3d.EXIT_CONVERGED, r
         ref = _oracle(rves[r["rve"]], r["load_case"])
