@@ -34,8 +34,9 @@ namespace {
 
 constexpr int kPartChoices[] = {1, 2, 4, 8, 16, 32, 64};
 constexpr int kMaxParts = 64;
-// Tile depths along z the autotuner tries (0: the rule of job_dims).
-constexpr int kTzChoices[] = {0, 16, 32};
+// Tile depths along z the autotuner tries (0: the rule of job_dims).  Each
+// candidate costs two timed launches per size class and k.
+constexpr int kTzChoices[] = {0, 32};
 constexpr unsigned long long kTimeoutNs = 120ull * 1000000000ull;
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
