@@ -52,7 +52,7 @@ EXPORTED_SYMBOLS = (
     "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
-    "e3d_device_bytes", "e3d_launch_count", "e3d_stencil_path", "e3d_probe_peaks", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_device_bytes", "e3d_launch_count", "e3d_stencil_path", "e3d_probe_peaks", "e3d_selftest_timeout", "e3d_strerror", "e3d_last_cuda_error",
     "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
     "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
@@ -158,6 +158,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_micro_ellipsoidal_pores_device.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
                                                      C.c_double, C.c_double, C.c_int32, C.c_uint64, C.c_int32, vp]
     L.e3d_upload_device.argtypes = [vp, vp, dp]
+    L.e3d_selftest_timeout.argtypes = [C.c_int32, C.c_int32, C.c_double]
     L.e3d_euler_to_rodrigues.argtypes = [C.c_int32, dp, dp]
     L.e3d_euler_to_rodrigues.restype = None
     for name in EXPORTED_SYMBOLS:

@@ -1020,6 +1020,51 @@ extern "C" int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* 
 }
 
 // ---------------------------------------------------------------------------
+// Failure-detection self-test: one kernel whose wait can never be satisfied --
+// a two-block grid barrier that block 1 never reaches, or an mbarrier phase
+// that expects 16 transaction bytes no copy will deliver -- and that must come
+// back through the bounded wait with DEV_TIMEOUT, leaving the context usable.
+namespace {
+
+__global__ void selftest_timeout_kernel(int which, GridBarrier* bar, int* err, unsigned long long timeout_ns) {
+  if (which == 0) {
+    if (blockIdx.x == 1) return;  // the partner that never arrives
+    (void)grid_barrier(bar, err, timeout_ns);
+  } else {
+    __shared__ uint64_t mb;
+    if (threadIdx.x == 0) {
+      mbar_init(&mb, 1);
+      fence_mbar_init();
+      mbar_arrive_expect_tx(&mb, 16);  // no copy will complete these bytes
+    }
+    __syncthreads();
+    if (!mbar_wait(&mb, 0, timeout_ns, err) && threadIdx.x == 0) atomicExch(err, DEV_TIMEOUT);
+  }
+}
+
+}  // namespace
+
+extern "C" int32_t e3d_selftest_timeout(int32_t device, int32_t which, double timeout_s) {
+  if ((which != 0 && which != 1) || !(timeout_s > 0.0) || timeout_s > 10.0) return E3D_ERR_INPUT;
+  E3D_CUDA(cudaSetDevice(device));
+  GridBarrier* bar = nullptr;
+  int* err = nullptr;
+  E3D_CUDA(cudaMalloc(&bar, sizeof(GridBarrier)));
+  E3D_CUDA(cudaMalloc(&err, sizeof(int)));
+  E3D_CUDA(cudaMemset(bar, 0, sizeof(GridBarrier)));
+  E3D_CUDA(cudaMemset(err, 0, sizeof(int)));
+  selftest_timeout_kernel<<<which == 0 ? 2 : 1, 32>>>(which, bar, err, (unsigned long long)(timeout_s * 1e9));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int derr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&derr, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(bar);
+  cudaFree(err);
+  if (e != cudaSuccess) return cuda_fail(e, "selftest");
+  return derr == DEV_TIMEOUT ? E3D_ERR_TIMEOUT : (derr == DEV_OK ? E3D_OK : E3D_ERR_CUDA);
+}
+
+// ---------------------------------------------------------------------------
 // Checkpoint / resume.  File: 16-byte header "E3DCKPT1" + version, the problem
 // dimensions and forms, gg0, the PcgState, then the state arrays and the
 // rel_res history (host byte order).

@@ -234,6 +234,14 @@ int32_t e3d_apply_noalloc(int32_t nx, int32_t ny, int32_t nz, int32_t nphase,
  * flops), the compute roofline denominators of the stencil. */
 int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops);
 
+/* Test hook (no counterpart in the reference): runs one kernel whose device
+ * wait can never be satisfied -- which = 0: a grid barrier whose partner block
+ * never arrives; which = 1: an mbarrier phase expecting bytes no copy delivers
+ * -- with a wall-clock limit of timeout_s seconds (at most 10).  Returns
+ * E3D_ERR_TIMEOUT when the wait ran out and was reported through the error flag
+ * (the context stays usable), any other status otherwise. */
+int32_t e3d_selftest_timeout(int32_t device, int32_t which, double timeout_s);
+
 const char* e3d_strerror(int32_t status);
 /* Text of the last CUDA error seen by any handle in this thread. */
 const char* e3d_last_cuda_error(void);
