@@ -369,7 +369,7 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------
-# The three added forms (the benchmark spec): full solves FP64 vs mixed, the batched
+# The three added forms: full solves FP64 vs mixed, the batched
 # effective-stiffness ensemble and the continuous-batching server.  Each prints
 # its own JSON line; the default run prints the plain-FP64 line above.
 def _full_solve(e3d, p, pix, rod, precision):
