@@ -112,10 +112,10 @@ struct ApplySmem {
 // TMA plane ring of the fused FP32 stencil.  One stage holds one node plane of
 // a tile: for h_old and z the main 32x8 box, the +x column box (4x8), the +y
 // row box (32x1) and the corner box (4x1), three components each, then the
-// tile's 32x8 phase ids.  Thread 0 keeps E3D_TMA_STAGES planes in flight,
+// tile's 32x8 phase ids.  Warp 0 keeps the ring full (one lane per box),
 // running ahead across the block's tiles; a stage is refilled once every
-// thread has read it (the __syncthreads after each commit), and consumers wait
-// on the stage's mbarrier with a wall-clock limit.
+// thread has read it (after the block barrier of the step that last reads it),
+// and consumers wait on the stage's mbarrier with a wall-clock limit.
 constexpr int kRingMain = 3 * 32 * 8 * 4;
 constexpr int kRingCol = 3 * 4 * 8 * 4;
 constexpr int kRingRow = 3 * 32 * 1 * 4;
@@ -127,8 +127,8 @@ constexpr unsigned kPlaneTx = 2u * (kRingMain + kRingCol + kRingRow + kRingCorne
 constexpr int kRingSmemBytes = E3D_TMA_STAGES * kStageBytes + 128;  // + alignment slack
 static_assert(kRingVec % 128 == 0 && kStageBytes % 128 == 0, "TMA destinations must stay 128-byte aligned");
 
-// Producer state, used by thread 0 only; kept in shared memory so it does not
-// occupy registers of every thread.
+// Producer state, written by lane 0 of warp 0 and read by warp 0; kept in
+// shared memory so it does not occupy registers of every thread.
 struct RingCursor {
   long long ptile, tstride, tend;
   const CUtensorMap* hmap;  // the four maps of the buffer read as h_old
