@@ -13,9 +13,15 @@
         implicit none
 
         integer(c_int32_t), parameter :: E3D_OK = 0
-        integer(c_int32_t), parameter :: E3D_ERR_MAXITER = 4
-        integer(c_int32_t), parameter :: E3D_CRIT_REF = 0
-        integer(c_int32_t), parameter :: E3D_PREC_FP64 = 0
+        integer(c_int32_t), parameter :: E3D_ERR_INPUT = 1, E3D_ERR_OOM = 2, E3D_ERR_BREAKDOWN = 3
+        integer(c_int32_t), parameter :: E3D_ERR_MAXITER = 4, E3D_ERR_TIMEOUT = 5, E3D_ERR_CUDA = 6
+        integer(c_int32_t), parameter :: E3D_ERR_STATE = 7
+        integer(c_int32_t), parameter :: E3D_EXIT_CONVERGED = 0, E3D_EXIT_HAH_GUARD = 1
+        integer(c_int32_t), parameter :: E3D_EXIT_MAXITER = 2, E3D_EXIT_BREAKDOWN = 3
+        integer(c_int32_t), parameter :: E3D_EXIT_TIMEOUT = 4, E3D_EXIT_RUNNING = 5
+        integer(c_int32_t), parameter :: E3D_CRIT_REF = 0, E3D_CRIT_PRECOND_REL = 1
+        integer(c_int32_t), parameter :: E3D_PRECOND_BLOCK_JACOBI = 0, E3D_PRECOND_NONE = 1
+        integer(c_int32_t), parameter :: E3D_PREC_FP64 = 0, E3D_PREC_MIXED = 1
 
         ! mirrors e3d_problem_t (field order and padding identical)
         type, bind(C) :: e3d_problem_t
@@ -59,6 +65,41 @@
           integer(c_int32_t) function e3d_femat(h) bind(C, name="e3d_femat")
             import :: c_ptr, c_int32_t
             type(c_ptr), value :: h
+          end function
+          integer(c_int32_t) function e3d_init_affine(h) bind(C, name="e3d_init_affine")
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+          end function
+          integer(c_int32_t) function e3d_solve_begin(h) bind(C, name="e3d_solve_begin")
+            import :: c_ptr, c_int32_t
+            type(c_ptr), value :: h
+          end function
+          integer(c_int32_t) function e3d_iterate(h, n, st) bind(C, name="e3d_iterate")
+            import :: c_ptr, c_int32_t, e3d_solve_stats_t
+            type(c_ptr), value :: h
+            integer(c_int32_t), value :: n
+            type(e3d_solve_stats_t), intent(out) :: st
+          end function
+          integer(c_int32_t) function e3d_run(h, utot, out12, st) bind(C, name="e3d_run")
+            import :: c_ptr, c_int32_t, c_double, e3d_solve_stats_t
+            type(c_ptr), value :: h
+            real(c_double), intent(out) :: utot(2), out12(12)
+            type(e3d_solve_stats_t), intent(out) :: st
+          end function
+          ! path: a C string, e.g. trim(name)//c_null_char
+          integer(c_int32_t) function e3d_checkpoint_save(h, path) bind(C, name="e3d_checkpoint_save")
+            import :: c_ptr, c_int32_t, c_char
+            type(c_ptr), value :: h
+            character(kind=c_char), intent(in) :: path(*)
+          end function
+          integer(c_int32_t) function e3d_checkpoint_load(h, path) bind(C, name="e3d_checkpoint_load")
+            import :: c_ptr, c_int32_t, c_char
+            type(c_ptr), value :: h
+            character(kind=c_char), intent(in) :: path(*)
+          end function
+          type(c_ptr) function e3d_strerror(status) bind(C, name="e3d_strerror")
+            import :: c_ptr, c_int32_t
+            integer(c_int32_t), value :: status
           end function
           integer(c_int32_t) function e3d_set_u(h, u) bind(C, name="e3d_set_u")
             import :: c_ptr, c_int32_t, c_double

@@ -64,3 +64,26 @@ def test_struct_layout_matches_header(lib):
     # e3d_problem_t: 14 int32/float (56 B) + 11 doubles (88 B) + int64 = 152 B
     assert C.sizeof(e3d.ProblemC) == 152
     assert C.sizeof(e3d.SolveStatsC) == 16 + 6 * 8
+
+
+def test_fortran_module_matches_the_c_abi():
+    """The iso_c_binding module (source only: no Fortran compiler here) names
+    only exported symbols and mirrors e3d_problem_t / e3d_solve_stats_t field
+    for field."""
+    import re
+
+    src = open(os.path.join(ROOT, "elas3d-xtal_gb300", "fortran", "elas3d_gpu_mod.f90")).read()
+    names = re.findall(r'bind\(C, name="(e3d_[A-Za-z0-9_]+)"\)', src)
+    assert names and set(names) <= set(e3d.EXPORTED_SYMBOLS)
+
+    def fortran_fields(tname):
+        body = src.split(f"type, bind(C) :: {tname}")[1].split("end type")[0]
+        out = []
+        for line in body.splitlines():
+            line = line.split("!")[0]
+            if "::" in line:
+                out += [re.sub(r"\(.*\)", "", f).strip() for f in line.split("::")[1].split(",")]
+        return out
+
+    assert fortran_fields("e3d_problem_t") == [f for f, _ in e3d.ProblemC._fields_]
+    assert fortran_fields("e3d_solve_stats_t") == [f for f, _ in e3d.SolveStatsC._fields_]
