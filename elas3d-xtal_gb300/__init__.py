@@ -40,7 +40,7 @@ E3D_ERR_TIMEOUT = 5
 E3D_ERR_CUDA = 6
 E3D_ERR_STATE = 7
 
-EXIT_CONVERGED, EXIT_HAH_GUARD, EXIT_MAXITER, EXIT_BREAKDOWN, EXIT_TIMEOUT, EXIT_RUNNING = range(6)
+EXIT_CONVERGED, EXIT_HAH_GUARD, EXIT_MAXITER, EXIT_BREAKDOWN, EXIT_TIMEOUT, EXIT_RUNNING, EXIT_CANCELLED = range(7)
 CRIT_REF, CRIT_PRECOND_REL = 0, 1
 PRECOND_BLOCK_JACOBI, PRECOND_NONE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -580,8 +580,8 @@ class ServeOptsC(C.Structure):
 
 BATCH_SYMBOLS = ("e3d_batch_opts_defaults", "e3d_batch_create", "e3d_batch_solve", "e3d_batch_results",
                  "e3d_batch_parts", "e3d_batch_destroy", "e3d_serve_opts_defaults", "e3d_serve_create",
-                 "e3d_serve_submit", "e3d_serve_step", "e3d_serve_result", "e3d_serve_memory",
-                 "e3d_serve_destroy")
+                 "e3d_serve_submit", "e3d_serve_step", "e3d_serve_result", "e3d_serve_cancel",
+                 "e3d_serve_memory", "e3d_serve_destroy")
 EXPORTED_SYMBOLS = EXPORTED_SYMBOLS + BATCH_SYMBOLS
 
 
@@ -603,6 +603,8 @@ def _bind_batch(L):
     L.e3d_serve_step.argtypes = [vp, ip]
     L.e3d_serve_result.argtypes = [vp, C.c_int64, C.POINTER(JobResultC)]
     L.e3d_serve_memory.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.e3d_serve_cancel.argtypes = [vp, C.c_int64]
+    L.e3d_serve_cancel.restype = C.c_int32
     L.e3d_serve_destroy.argtypes = [vp]
     L._e3d_batch_bound = True
     return L
@@ -709,6 +711,10 @@ class Server:
             return None
         _check(rc, "e3d_serve_result")
         return r.as_dict()
+
+    def cancel(self, rid: int):
+        """Withdraw a queued or active request (between steps)."""
+        _check(self.L.e3d_serve_cancel(self._h, int(rid)), "e3d_serve_cancel")
 
     def memory(self):
         a, b = C.c_int64(), C.c_int64()

@@ -15,6 +15,7 @@
 #include "e3d_batch.h"
 #include "e3d_gpu.h"
 #include "e3d_jobs.cuh"
+#include "e3d_trace.h"
 
 using namespace e3d;
 
@@ -479,6 +480,7 @@ int32_t e3d_batch_destroy(e3d_batch_t* b) {
 }
 
 int32_t e3d_batch_create(e3d_batch_t** out, const e3d_rve_t* rves, int32_t n, const e3d_batch_opts_t* o) {
+  E3D_TRACE("e3d_batch_create");
   if (!out || !rves || n < 1 || !o) return E3D_ERR_INPUT;
   *out = nullptr;
   const int mask = o->load_cases ? o->load_cases : 0x3f;
@@ -573,6 +575,7 @@ int32_t e3d_batch_create(e3d_batch_t** out, const e3d_rve_t* rves, int32_t n, co
 }
 
 int32_t e3d_batch_solve(e3d_batch_t* b, double* ceff, double* seconds) {
+  E3D_TRACE("e3d_batch_solve");
   if (!b) return E3D_ERR_INPUT;
   cudaSetDevice(b->device);
   cudaEvent_t e0, e1;
@@ -755,6 +758,7 @@ int32_t e3d_serve_submit(e3d_server_t* s, const e3d_rve_t* rve, const double str
 }
 
 int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
+  E3D_TRACE("e3d_serve_step");
   if (!s) return E3D_ERR_INPUT;
   cudaSetDevice(s->device);
   // admit in arrival order while slots and budget allow
@@ -852,6 +856,49 @@ int32_t e3d_serve_result(e3d_server_t* s, int64_t id, e3d_job_result_t* out) {
   if (it == s->finished.end()) return E3D_ERR_STATE;
   *out = it->second->result;
   return E3D_OK;
+}
+
+int32_t e3d_serve_cancel(e3d_server_t* s, int64_t id) {
+  E3D_TRACE("e3d_serve_cancel");
+  if (!s) return E3D_ERR_INPUT;
+  if (s->finished.count(id)) return E3D_ERR_STATE;
+  cudaSetDevice(s->device);
+  auto finish = [&](ServeJob* j, int iterations) {
+    e3d_job_result_t& o = j->result;
+    std::memset(&o, 0, sizeof o);
+    o.rve = -1;
+    o.load_case = -1;
+    o.status = E3D_EXIT_CANCELLED;
+    o.iterations = iterations;
+    o.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - j->t_submit).count();
+    j->done = true;
+    j->pix.clear();
+    j->pix.shrink_to_fit();
+    s->finished[j->id] = j;
+  };
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+    if ((*it)->id == id) {
+      ServeJob* j = *it;
+      s->queue.erase(it);
+      finish(j, 0);
+      return E3D_OK;
+    }
+  for (auto it = s->active.begin(); it != s->active.end(); ++it)
+    if ((*it)->id == id) {
+      ServeJob* j = *it;
+      PcgState st{};
+      BCUDA(cudaMemcpyAsync(&st, j->J.d.st, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+      BCUDA(cudaStreamSynchronize(s->stream));
+      int stage = 0;
+      BCUDA(cudaMemcpy(&stage, j->J.d.stage, 4, cudaMemcpyDeviceToHost));
+      BCUDA(cudaFreeAsync(j->mem, s->stream));
+      j->mem = nullptr;
+      s->bytes_now -= (int64_t)j->bytes;
+      s->active.erase(it);
+      finish(j, stage == JOB_NEW ? 0 : st.it);
+      return E3D_OK;
+    }
+  return E3D_ERR_INPUT;
 }
 
 int32_t e3d_serve_memory(e3d_server_t* s, int64_t* now, int64_t* peak) {

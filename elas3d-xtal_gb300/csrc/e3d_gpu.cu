@@ -16,6 +16,7 @@
 
 #include "e3d_gpu.h"
 #include "e3d_kernels.cuh"
+#include "e3d_trace.h"
 
 using namespace e3d;
 
@@ -427,6 +428,7 @@ int32_t e3d_stencil_path(const e3d_handle_t* h) {
 }
 
 int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
+  E3D_TRACE("e3d_upload");
   if (!h || !pix) return E3D_ERR_INPUT;
   const auto& p = h->prob;
   if (p.flag_m == 1 && p.nphase > 1 && !rod) return E3D_ERR_INPUT;
@@ -453,6 +455,7 @@ int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
 }
 
 int32_t e3d_upload_device(e3d_handle_t* h, const int32_t* d_pix, const double* rod) {
+  E3D_TRACE("e3d_upload_device");
   if (!h || !d_pix) return E3D_ERR_INPUT;
   const auto& p = h->prob;
   if (p.flag_m == 1 && p.nphase > 1 && !rod) return E3D_ERR_INPUT;
@@ -479,6 +482,7 @@ int32_t e3d_upload_device(e3d_handle_t* h, const int32_t* d_pix, const double* r
 }
 
 int32_t e3d_femat(e3d_handle_t* h) {
+  E3D_TRACE("e3d_femat");
   if (!h) return E3D_ERR_INPUT;
   if (!h->uploaded) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -518,6 +522,7 @@ int32_t e3d_femat(e3d_handle_t* h) {
 }
 
 int32_t e3d_init_affine(e3d_handle_t* h) {
+  E3D_TRACE("e3d_init_affine");
   if (!h) return E3D_ERR_INPUT;
   cudaSetDevice(h->device);
   affine_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->J, h->u);
@@ -527,6 +532,7 @@ int32_t e3d_init_affine(e3d_handle_t* h) {
 }
 
 int32_t e3d_energy(e3d_handle_t* h, double* utot, double* gg) {
+  E3D_TRACE("e3d_energy");
   if (!h) return E3D_ERR_INPUT;
   if (!h->femat_done) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -548,6 +554,7 @@ int32_t e3d_energy(e3d_handle_t* h, double* utot, double* gg) {
 }
 
 int32_t e3d_solve_begin(e3d_handle_t* h) {
+  E3D_TRACE("e3d_solve_begin");
   if (!h) return E3D_ERR_INPUT;
   if (!h->energy_done) return E3D_ERR_STATE;
   const bool mixed = h->prob.precision == E3D_PREC_MIXED;
@@ -719,6 +726,7 @@ int32_t residual_replacement(e3d_handle* h) {
 extern "C" {
 
 int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
+  E3D_TRACE("e3d_iterate");
   if (!h || n < 0) return E3D_ERR_INPUT;
   if (!h->solve_ready) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -782,6 +790,7 @@ int32_t e3d_solve(e3d_handle_t* h, e3d_solve_stats_t* st) {
 }
 
 int32_t e3d_stress(e3d_handle_t* h, double strav[6], double epsav[6]) {
+  E3D_TRACE("e3d_stress");
   if (!h) return E3D_ERR_INPUT;
   if (!h->femat_done) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -800,6 +809,7 @@ int32_t e3d_stress(e3d_handle_t* h, double strav[6], double epsav[6]) {
 }
 
 int32_t e3d_stress_field(e3d_handle_t* h, double* sigma, double* vm) {
+  E3D_TRACE("e3d_stress_field");
   if (!h) return E3D_ERR_INPUT;
   if (!h->femat_done) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -829,6 +839,7 @@ int32_t e3d_stress_field(e3d_handle_t* h, double* sigma, double* vm) {
 }
 
 int32_t e3d_run(e3d_handle_t* h, double utot[2], double out12[12], e3d_solve_stats_t* st) {
+  E3D_TRACE("e3d_run");
   if (!h) return E3D_ERR_INPUT;
   int32_t rc;
   if ((rc = e3d_femat(h))) return rc;
@@ -1098,6 +1109,7 @@ int32_t ckpt_read(FILE* f, T* dev, size_t count, cudaStream_t s) {
 }  // namespace
 
 extern "C" int32_t e3d_checkpoint_save(e3d_handle_t* h, const char* path) {
+  E3D_TRACE("e3d_checkpoint_save");
   if (!h || !path) return E3D_ERR_INPUT;
   if (!h->solve_ready) return E3D_ERR_STATE;
   cudaSetDevice(h->device);
@@ -1140,6 +1152,7 @@ extern "C" int32_t e3d_checkpoint_save(e3d_handle_t* h, const char* path) {
 }
 
 extern "C" int32_t e3d_checkpoint_load(e3d_handle_t* h, const char* path) {
+  E3D_TRACE("e3d_checkpoint_load");
   if (!h || !path) return E3D_ERR_INPUT;
   if (!h->femat_done) return E3D_ERR_STATE;
   cudaSetDevice(h->device);

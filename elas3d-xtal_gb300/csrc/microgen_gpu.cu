@@ -21,6 +21,7 @@
 
 #include "e3d_micro.h"
 #include "microgen_plan.h"
+#include "e3d_trace.h"
 
 void e3d_record_cuda_error(const char* what, cudaError_t e);
 
@@ -252,6 +253,7 @@ done:
 extern "C" int32_t e3d_micro_grains_device(int32_t nx, int32_t ny, int32_t nz, int32_t ngrains,
                                            double laguerre_sigma, uint64_t seed, int32_t device, int32_t* d_pix,
                                            double* rod) {
+  E3D_TRACE("e3d_micro_grains_device");
   if (nx <= 0 || ny <= 0 || nz <= 0 || ngrains <= 0 || !d_pix || !rod) return -1;
   GrainPlan P;
   int32_t rc = grain_plan(nx, ny, nz, ngrains, laguerre_sigma, seed, rod, P);
@@ -324,6 +326,7 @@ done:
 extern "C" int32_t e3d_micro_spherical_pores_device(int32_t nx, int32_t ny, int32_t nz, double target_frac,
                                                     double log_mu, double log_sigma, int32_t pore_phase,
                                                     uint64_t seed, int32_t device, int32_t* d_pix) {
+  E3D_TRACE("e3d_micro_spherical_pores_device");
   return add_pores_device(0, nx, ny, nz, target_frac, 1.0, log_mu, log_sigma, pore_phase, seed, device, d_pix);
 }
 
@@ -331,5 +334,6 @@ extern "C" int32_t e3d_micro_ellipsoidal_pores_device(int32_t nx, int32_t ny, in
                                                       double aspect, double log_mu, double log_sigma,
                                                       int32_t pore_phase, uint64_t seed, int32_t device,
                                                       int32_t* d_pix) {
+  E3D_TRACE("e3d_micro_ellipsoidal_pores_device");
   return add_pores_device(1, nx, ny, nz, target_frac, aspect, log_mu, log_sigma, pore_phase, seed, device, d_pix);
 }

@@ -36,6 +36,7 @@ void usage() {
       "  --flag-m 0|1              0: isotropic matrix, 1: rotated cubic grains (1)\n"
       "  --outdir DIR              output directory (.)\n"
       "  --fullfield               also write fullfield_poly.bin\n"
+      "  --json                    print one JSON metrics line for the solve on stdout\n"
       "  --checkpoint FILE         save the PCG state at exit (resume with --resume)\n"
       "  --resume FILE             continue a saved solve\n"
       "  --device N                CUDA device (0)\n");
@@ -60,7 +61,7 @@ int main(int argc, char** argv) {
   float tol = 1.0e-8f;
   int max_iter = 10000, precision = E3D_PREC_FP64, criterion = E3D_CRIT_REF, device = 0, flag_m = 1;
   int precond = E3D_PRECOND_BLOCK_JACOBI;
-  bool fullfield = false;
+  bool fullfield = false, json = false;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto need = [&](int k) {
@@ -117,6 +118,8 @@ int main(int argc, char** argv) {
     } else if (a == "--outdir") {
       need(1);
       outdir = argv[++i];
+    } else if (a == "--json") {
+      json = true;
     } else if (a == "--fullfield") {
       fullfield = true;
     } else if (a == "--checkpoint") {
@@ -256,6 +259,34 @@ int main(int argc, char** argv) {
   const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   std::fprintf(out, "\n Calculation complete!\n Total calculation time: %f seconds\n", elapsed);
   std::printf(" End of CG\n\n Calculation complete!\n Total calculation time: %f seconds\n", elapsed);
+  if (json) {  // one metrics line per solve (non-finite values as null)
+    auto num = [](double v) {
+      char b[40];
+      if (std::isfinite(v))
+        std::snprintf(b, sizeof b, "%.17g", v);
+      else
+        std::snprintf(b, sizeof b, "null");
+      return std::string(b);
+    };
+    std::string line = "{\"grid\": [" + std::to_string(nx) + ", " + std::to_string(ny) + ", " + std::to_string(nz) +
+                       "], \"dof\": " + std::to_string(3 * ns) + ", \"precision\": \"" +
+                       (precision == E3D_PREC_MIXED ? "mixed" : "fp64") + "\", \"criterion\": \"" +
+                       (criterion == E3D_CRIT_PRECOND_REL ? "precond" : "ref") + "\", \"iterations\": " +
+                       std::to_string(st.iterations) + ", \"exit_reason\": " + std::to_string(st.exit_reason) +
+                       ", \"refinements\": " + std::to_string(st.refinements) + ", \"resets\": " +
+                       std::to_string(st.resets) + ", \"utot0\": " + num(utot0) + ", \"utot\": " + num(utot) +
+                       ", \"rel_res\": " + num(st.rel_res) + ", \"true_rel\": " + num(st.true_rel) +
+                       ", \"ms_setup\": " + num(st.ms_setup) + ", \"ms_pcg\": " + num(st.ms_iter) +
+                       ", \"seconds_total\": " + num(elapsed) + ", \"dof_iters_per_s\": " +
+                       num(st.ms_iter > 0 ? 3.0 * (double)ns * st.iterations / (st.ms_iter * 1e-3) : 0.0);
+    line += ", \"strav\": [";
+    for (int k = 0; k < 6; ++k) line += num(strav[k]) + (k < 5 ? ", " : "]");
+    line += ", \"epsav\": [";
+    for (int k = 0; k < 6; ++k) line += num(epsav[k]) + (k < 5 ? ", " : "]");
+    line += "}";
+    std::printf("%s\n", line.c_str());
+    std::fflush(stdout);
+  }
   std::fclose(out);
   if (fullfield) {  // stress_fullfield_OpenMP (:2639-2877) with a raw file instead of HDF5
     std::vector<double> sig(6 * (size_t)ns), vm((size_t)ns);

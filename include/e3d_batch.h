@@ -115,6 +115,14 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending);
 /* Result of a finished request (E3D_ERR_STATE while it is not finished). */
 int32_t e3d_serve_result(e3d_server_t* s, int64_t id, e3d_job_result_t* out);
 
+/* Cancels a request between rounds: a queued request leaves the queue, an
+ * active one gives its slot and device memory back before the next round.  Its
+ * result then has status E3D_EXIT_CANCELLED (iterations done so far).
+ * E3D_ERR_STATE if the request already finished, E3D_ERR_INPUT for an unknown
+ * id. */
+#define E3D_EXIT_CANCELLED 6
+int32_t e3d_serve_cancel(e3d_server_t* s, int64_t id);
+
 /* Bytes of device memory held now / at most so far. */
 int32_t e3d_serve_memory(e3d_server_t* s, int64_t* now, int64_t* peak);
 

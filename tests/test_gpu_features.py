@@ -82,7 +82,7 @@ def test_driver_end_to_end(tmp_path):
     pix, rod = e3d.micro_grains(14, 14, 14, 6, 4)
     inp = str(tmp_path / "in.e3d")
     e3d.micro_write(inp, pix, rod, (14, 14, 14))
-    out = subprocess.run([drv, "--input", inp, "--outdir", str(tmp_path), "--fullfield",
+    out = subprocess.run([drv, "--input", inp, "--outdir", str(tmp_path), "--fullfield", "--json",
                           "--strain", "1e-3", "0", "0", "0", "0", "0"], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
     for f in ("output_SS316L_polycrystal.txt", "cg_history_polycrystal.txt", "cgitr_SS316L_polycrystal.txt",
@@ -94,5 +94,11 @@ def test_driver_end_to_end(tmp_path):
     assert f"Number of conjugate steps= {ref['lstep']}" in log or "Number of conjugate steps=" in log
     energy = float(log.split(" Energy=")[1].split()[0])
     assert abs(energy - ref["utot"]) <= 1e-9 * abs(ref["utot"])
+    import json
+
+    metrics = json.loads([ln for ln in out.stdout.splitlines() if ln.startswith("{")][-1])
+    assert metrics["utot"] == pytest.approx(ref["utot"], rel=1e-9)
+    assert metrics["iterations"] == int(log.split("Number of conjugate steps=")[1].split()[0])
+    assert metrics["dof"] == 3 * 14 ** 3 and metrics["precision"] == "fp64"
     raw = np.fromfile(tmp_path / "fullfield_poly.bin", dtype=np.uint8)
     assert raw.size == 8 + 16 + 4 * 14 ** 3 + 8 * 14 ** 3 * 7

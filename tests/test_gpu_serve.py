@@ -76,3 +76,25 @@ def test_serve_hbm_budget_bounds_admission():
         now, peak = srv.memory()
     assert all(r is not None and r["status"] == e3d.EXIT_CONVERGED for r in out)
     assert peak <= budget and now == 0
+
+
+def test_serve_cancel_queued_and_active_requests():
+    reqs = _requests()
+    with e3d.Server(round_iters=5, max_active=2) as srv:
+        ids = [srv.submit(*r) for r in reqs[:4]]
+        srv.step()  # requests 0 and 1 active, 2 and 3 queued
+        srv.cancel(ids[1])  # active
+        srv.cancel(ids[3])  # queued
+        with pytest.raises(e3d.E3DError):
+            srv.cancel(12345)  # unknown id
+        out = _drain(srv, ids)
+        now, _ = srv.memory()
+        with pytest.raises(e3d.E3DError):
+            srv.cancel(ids[0])  # already finished
+    assert out[1]["status"] == e3d.EXIT_CANCELLED and out[1]["iterations"] > 0
+    assert out[3]["status"] == e3d.EXIT_CANCELLED and out[3]["iterations"] == 0
+    for k in (0, 2):
+        assert out[k]["status"] == e3d.EXIT_CONVERGED
+        ref = _oracle(*reqs[k])
+        assert abs(out[k]["utot"] - ref["utot"]) <= ENERGY_TOL * abs(ref["utot"])
+    assert now == 0
