@@ -9,7 +9,8 @@ distributions of that configuration.  One step = one PCG iteration
 (apply + dot products + updates).
 
   value : device-resident state, K iterations timed with CUDA events on the
-          library's stream (vectors are 3 GB each, far larger than L2)
+          library's stream (an iteration streams 364 B per node in FP64, 184
+          in the mixed form: 45 / 23 GB at 500^3, far more than the L2 holds)
   e2e   : the same metric through the C ABI from pinned host buffers: upload,
           femat, affine guess, energy, block-Jacobi, K iterations, stress and
           the download of u are all inside the timed region
@@ -345,7 +346,8 @@ def run_ours(args):
                    "precision": "mixed (FP64 residual replacement every 50 iterations)" if mixed else "fp64",
                    "stencil_path": path, "criterion": "reference (sqrt(z.g/|g0|^2))",
                    "step": "one PCG iteration (fused apply + updates, persistent kernel)",
-                   "l2": "inputs larger than L2 (3 GB per vector)", "parallelism": f"replicas x{ws}",
+                   "l2": f"each iteration streams {bytes_node * ns / 1e9:.2f} GB, more than the 126 MB L2 holds",
+                   "parallelism": f"replicas x{ws}",
                    "e2e": "C-ABI calls from pinned host buffers: upload..K iterations..stress, get_u"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": roof,
         "wall_ms_per_step": wall / K * 1e3,

@@ -29,7 +29,10 @@ from dataclasses import dataclass, field
 import numpy as np
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "_build", "libe3d_gpu.so")
+# E3D_LIBRARY selects another build of the same library, e.g. the
+# bounds-checked debug variant BOUNDS_LIB_PATH (build.py --bounds).
+LIB_PATH = os.environ.get("E3D_LIBRARY") or os.path.join(_PKG, "_build", "libe3d_gpu.so")
+BOUNDS_LIB_PATH = os.path.join(_PKG, "_build", "bounds", "libe3d_gpu_bounds.so")
 
 E3D_OK = 0
 E3D_ERR_INPUT = 1
@@ -52,7 +55,8 @@ EXPORTED_SYMBOLS = (
     "e3d_stress", "e3d_stress_field", "e3d_run", "e3d_apply", "e3d_apply_device",
     "e3d_set_u", "e3d_get_u", "e3d_get_g", "e3d_get_b", "e3d_get_C", "e3d_get_cmod",
     "e3d_get_dk", "e3d_get_minv", "e3d_get_history", "e3d_device_ptrs",
-    "e3d_device_bytes", "e3d_launch_count", "e3d_stencil_path", "e3d_probe_peaks", "e3d_selftest_timeout", "e3d_strerror", "e3d_last_cuda_error",
+    "e3d_device_bytes", "e3d_launch_count", "e3d_stencil_path", "e3d_probe_peaks", "e3d_selftest_timeout",
+    "e3d_debug_bounds", "e3d_selftest_bounds", "e3d_strerror", "e3d_last_cuda_error",
     "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
     "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
@@ -159,6 +163,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                                      C.c_double, C.c_double, C.c_int32, C.c_uint64, C.c_int32, vp]
     L.e3d_upload_device.argtypes = [vp, vp, dp]
     L.e3d_selftest_timeout.argtypes = [C.c_int32, C.c_int32, C.c_double]
+    L.e3d_debug_bounds.argtypes = [C.POINTER(C.c_int64)]
+    L.e3d_selftest_bounds.argtypes = [C.c_int32]
     L.e3d_euler_to_rodrigues.argtypes = [C.c_int32, dp, dp]
     L.e3d_euler_to_rodrigues.restype = None
     for name in EXPORTED_SYMBOLS:
@@ -506,6 +512,18 @@ def probe_peaks(device: int = 0):
     a, b = C.c_double(), C.c_double()
     _check(load_library().e3d_probe_peaks(device, C.byref(a), C.byref(b)), "e3d_probe_peaks")
     return a.value, b.value
+
+
+def debug_bounds() -> dict | None:
+    """Record of the bounds-checked debug build (e3d_debug_bounds), cleared on
+    read: {"count", "unit", "line", "index", "limit"}; None when the loaded
+    library was built without the checks."""
+    rep = (C.c_int64 * 5)()
+    rc = load_library().e3d_debug_bounds(rep)
+    if rc == E3D_ERR_STATE:
+        return None
+    _check(rc, "e3d_debug_bounds")
+    return dict(zip(("count", "unit", "line", "index", "limit"), (int(v) for v in rep)))
 
 
 def micro_write(path, pix, rod, shape):

@@ -5,6 +5,11 @@ Produces ``elas3d-xtal_gb300/_build/libe3d_gpu.so`` from
 ``csrc/microgen.cpp`` (g++, portable flags so the same recipe builds on x86-64
 and AArch64).  Translation units compile in parallel; the step is skipped when
 the library is newer than every source.
+
+``build(bounds=True)`` makes the bounds-checked debug variant,
+``_build/bounds/libe3d_gpu_bounds.so``: the same sources compiled with
+``-DE3D_BOUNDS`` (every checked index compared with its buffer's length and
+recorded, never trapping; ``e3d_debug_bounds`` reads the record).
 """
 from __future__ import annotations
 
@@ -21,6 +26,8 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libe3d_gpu.so")
 DRIVER = os.path.join(OUT, "e3d_run")
+BOUNDS_OUT = os.path.join(OUT, "bounds")
+BOUNDS_LIB = os.path.join(BOUNDS_OUT, "libe3d_gpu_bounds.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -39,24 +46,27 @@ def _sources():
            [os.path.join(drv, f) for f in sorted(os.listdir(drv)) if f.endswith(".cpp")]
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB) or not os.path.exists(DRIVER):
+def up_to_date(bounds: bool = False) -> bool:
+    targets = [BOUNDS_LIB] if bounds else [LIB, DRIVER]
+    if not all(os.path.exists(t) for t in targets):
         return False
-    t = min(os.path.getmtime(LIB), os.path.getmtime(DRIVER))
+    t = min(os.path.getmtime(t) for t in targets)
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(OUT, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, bounds: bool = False) -> str:
+    lib = BOUNDS_LIB if bounds else LIB
+    if not force and up_to_date(bounds):
+        return lib
+    out = BOUNDS_OUT if bounds else OUT
+    os.makedirs(out, exist_ok=True)
     nvcc = _nvcc()
     cu_units = ["e3d_gpu", "e3d_noalloc", "e3d_batch", "microgen_gpu"]
-    cu_objs = [os.path.join(OUT, u + ".o") for u in cu_units]
-    cpp_obj = os.path.join(OUT, "microgen.o")
+    cu_objs = [os.path.join(out, u + ".o") for u in cu_units]
+    cpp_obj = os.path.join(out, "microgen.o")
     cu_cmds = []
     for u, o in zip(cu_units, cu_objs):
-        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *(["-DE3D_BOUNDS"] if bounds else []),
                "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, u + ".cu"), "-o", o]
         if ptxas_info:
             cmd[1:1] = ["-Xptxas", "-v"]
@@ -72,9 +82,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     with ThreadPoolExecutor(len(cu_cmds) + 1) as ex:
         logs = list(ex.map(run, [*cu_cmds, cpp_cmd]))
-    link = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *cu_objs, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
+    link = [nvcc, *ARCH, "-shared", "-o", lib + ".tmp", *cu_objs, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
     logs.append(run(link))
-    os.replace(LIB + ".tmp", LIB)
+    os.replace(lib + ".tmp", lib)
+    if bounds:
+        if verbose or ptxas_info:
+            sys.stdout.write("".join(logs))
+        return lib
     # command-line driver (mirrors `program elas3d`), linked against the library
     drv = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, os.path.join(PKG, "driver", "e3d_run.cpp"),
            "-L", OUT, "-le3d_gpu", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
@@ -86,5 +100,4 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True, ptxas_info="-v" in sys.argv)
-    print(LIB)
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="-v" in sys.argv, bounds="--bounds" in sys.argv))

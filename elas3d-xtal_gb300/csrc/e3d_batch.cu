@@ -311,6 +311,7 @@ struct Engine {
     E.part_job = d_part_job;
     E.part_rank = d_part_rank;
     E.nparts_total = nparts_total;
+    E.njobs = njobs;
     E.head = d_head;
     E.err = d_err;
     E.it_limit = it_limit;
@@ -909,3 +910,6 @@ int32_t e3d_serve_memory(e3d_server_t* s, int64_t* now, int64_t* peak) {
 }
 
 }  // extern "C"
+
+// Bounds-checked build: this translation unit's record (read by e3d_debug_bounds).
+int e3d_bounds_take_batch(long long out[4]) { return e3d::bounds_take(out); }

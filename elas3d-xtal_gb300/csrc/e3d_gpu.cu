@@ -218,6 +218,7 @@ ApplyArgs<double> apply_args(e3d_handle* h, const double* x, double* y) {
   A.g = h->G;
   A.pix = h->pix;
   A.cs = h->cs;
+  A.ncs = h->prob.nphase;
   A.x = x;
   A.zv = nullptr;
   A.gamma = 0.0;
@@ -382,10 +383,11 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
     if ((e = cudaMemsetAsync(h->h32a, 0, sizeof(float) * n3, h->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(h->h32b, 0, sizeof(float) * n3, h->stream)) != cudaSuccess)
       return fail(cuda_fail(e, "memset"));
-    // TMA-fed inner stencil where the grid allows it (E3D_NO_TMA=1 keeps per-thread loads)
-    const char* no_tma = std::getenv("E3D_NO_TMA");
+    // Inner stencil: per-thread loads (500^3: 6.9 ms per inner iteration, the
+    // TMA plane ring 8.0 ms); E3D_TMA=1 selects the ring where the grid allows it.
+    const char* want_tma = std::getenv("E3D_TMA");
     PlaneMaps hm{};
-    if (!(no_tma && no_tma[0] && no_tma[0] != '0') && per_sm_tma >= 1 &&
+    if (want_tma && want_tma[0] && want_tma[0] != '0' && per_sm_tma >= 1 &&
         e3d_encode_plane_maps(&hm, h->h32a, h->h32b, h->z32, h->pix, h->G)) {
       if ((rc = dalloc(h, &h->maps, 1))) return fail(rc);
       if ((e = cudaMemcpyAsync(h->maps, &hm, sizeof hm, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
@@ -653,6 +655,7 @@ PcgArgs<float> pcg_args<float>(e3d_handle* h) {
   P.A.g = h->G;
   P.A.pix = h->pix;
   P.A.cs = h->cs32;
+  P.A.ncs = h->prob.nphase;
   P.A.hx = reinterpret_cast<float*>(h->hx);  // the FP64 halo buffers, reused
   P.A.hy = reinterpret_cast<float*>(h->hy);
   P.A.hd = reinterpret_cast<float*>(h->hd);
@@ -1073,6 +1076,60 @@ extern "C" int32_t e3d_selftest_timeout(int32_t device, int32_t which, double ti
   cudaFree(err);
   if (e != cudaSuccess) return cuda_fail(e, "selftest");
   return derr == DEV_TIMEOUT ? E3D_ERR_TIMEOUT : (derr == DEV_OK ? E3D_OK : E3D_ERR_CUDA);
+}
+
+// ---------------------------------------------------------------------------
+// Bounds-checked debug build: each translation unit keeps its own record.
+int e3d_bounds_take_batch(long long out[4]);    // e3d_batch.cu
+int e3d_bounds_take_noalloc(long long out[4]);  // e3d_noalloc.cu
+
+#ifdef E3D_BOUNDS
+namespace {
+// Thread 5 asks for element 37 of a 32-element buffer; the check sends it to 0.
+__global__ void selftest_bounds_kernel(int* buf, int n) {
+  const int i = (int)threadIdx.x + (threadIdx.x == 5 ? n : 0);
+  buf[E3D_IDX(i, n)] = 1;
+}
+}  // namespace
+#endif
+
+extern "C" int32_t e3d_debug_bounds(int64_t report[5]) {
+  if (!report) return E3D_ERR_INPUT;
+  long long r[3][4];
+  const int k[3] = {e3d::bounds_take(r[0]), e3d_bounds_take_batch(r[1]), e3d_bounds_take_noalloc(r[2])};
+  for (int i = 0; i < 5; ++i) report[i] = 0;
+  for (int u = 0; u < 3; ++u) {
+    if (k[u] < 0) return cuda_fail(cudaGetLastError(), "e3d_debug_bounds");
+    if (r[u][0] > 0 && report[0] == 0) {
+      report[1] = u;
+      report[2] = r[u][1];
+      report[3] = r[u][2];
+      report[4] = r[u][3];
+    }
+    report[0] += r[u][0];
+  }
+  return k[0] == 1 ? E3D_OK : E3D_ERR_STATE;
+}
+
+extern "C" int32_t e3d_selftest_bounds(int32_t device) {
+#ifdef E3D_BOUNDS
+  E3D_CUDA(cudaSetDevice(device));
+  int64_t rep[5];
+  int32_t rc = e3d_debug_bounds(rep);  // clear
+  if (rc) return rc;
+  int* buf = nullptr;
+  E3D_CUDA(cudaMalloc(&buf, 32 * sizeof(int)));
+  selftest_bounds_kernel<<<1, 32>>>(buf, 32);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(e, "selftest_bounds");
+  if ((rc = e3d_debug_bounds(rep))) return rc;
+  return (rep[0] == 1 && rep[1] == 0 && rep[3] == 37 && rep[4] == 32) ? E3D_OK : E3D_ERR_CUDA;
+#else
+  (void)device;
+  return E3D_ERR_STATE;
+#endif
 }
 
 // ---------------------------------------------------------------------------

@@ -76,6 +76,7 @@ struct EngineArgs {
   const int* part_job;   // part index -> job
   const int* part_rank;  // part index -> rank within its job
   int nparts_total;
+  int njobs;
   unsigned int* head;    // dispenser
   int* err;
   int it_limit;          // iterations per job per launch
@@ -121,14 +122,19 @@ static __device__ bool job_barrier(GridBarrier* gb, unsigned int k, int* err, un
   return s_ok != 0;
 }
 
+// Slots of the per-job partial array.
+enum : int { SL_A = 0, SL_B = 1, SL_C = 2, SL_U = 3, SL_GG = 4, SL_ZG = 5, SL_S = 6 /* 6..17 */ };
+constexpr int kJobSlots = 18;
+
 // Sum of the k partials of slot `slot`, same value in every part.
 static __device__ double job_reduce(const JobDesc& J, int slot, double* red) {
-  return reduce_broadcast(J.partial + (long long)slot * J.nparts, J.nparts, red);
+  return reduce_broadcast(J.partial + E3D_IDX((long long)slot * J.nparts, kJobSlots * (long long)J.nparts), J.nparts,
+                          red);
 }
 
 static __device__ void job_put(const JobDesc& J, int slot, int part, double v, double* red) {
   const double s = block_sum<NT>(v, red);
-  if (threadIdx.x == 0) J.partial[(long long)slot * J.nparts + part] = s;
+  if (threadIdx.x == 0) J.partial[E3D_IDX((long long)slot * J.nparts + part, kJobSlots * (long long)J.nparts)] = s;
 }
 
 // Visits every node of the part's tiles in tile order: f(m, x, y, z, tix, tiy, tiz, lx, ly, lz).
@@ -145,7 +151,8 @@ __device__ __forceinline__ void for_part_nodes(const JobDesc& J, int part, F&& f
     const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
     if (tx >= wx || ty >= wy) continue;
     const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
-    for (int lz = 0; lz < wz; ++lz) f(col + nxy * (z0 + lz), x0 + tx, y0 + ty, z0 + lz, tix, tiy, tiz, tx, ty, lz);
+    for (int lz = 0; lz < wz; ++lz)
+      f(E3D_IDX(col + nxy * (z0 + lz), G.ns), x0 + tx, y0 + ty, z0 + lz, tix, tiy, tiz, tx, ty, lz);
   }
 }
 
@@ -162,8 +169,8 @@ static __device__ __noinline__ void job_b_node(const JobDesc& J, int x, int y, i
     bool any;
     element_delta(G, J.J, ex, ey, ez, d, any);
     if (!any) continue;
-    const int ph = J.pix[(long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez];
-    const double* D = J.dk + (long long)ph * 576;
+    const int ph = J.pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
+    const double* D = J.dk + E3D_IDX(ph, J.nphase_total) * 576;
     for (int i = 0; i < 3; ++i) {
       double s = 0.0;
       for (int rb = 0; rb < 8; ++rb)
@@ -179,8 +186,8 @@ static __device__ __noinline__ double job_c_elem(const JobDesc& J, int x, int y,
   double d[8][3];
   bool any;
   element_delta(G, J.J, x, y, z, d, any);
-  const int ph = J.pix[(long long)x + (long long)G.nx * y + (long long)G.nx * G.ny * z];
-  const double* D = J.dk + (long long)ph * 576;
+  const int ph = J.pix[E3D_IDX((long long)x + (long long)G.nx * y + (long long)G.nx * G.ny * z, G.ns)];
+  const double* D = J.dk + E3D_IDX(ph, J.nphase_total) * 576;
   double e = 0.0;
   for (int r = 0; r < 24; ++r) {
     double s = 0.0;
@@ -199,6 +206,7 @@ inline __device__ ApplyArgs<double> job_apply_args<double>(const JobDesc& J) {
   A.g = J.G;
   A.pix = J.pix;
   A.cs = J.cs64;
+  A.ncs = J.nphase_total;
   A.hx = J.hx;
   A.hy = J.hy;
   A.hd = J.hd;
@@ -211,15 +219,13 @@ inline __device__ ApplyArgs<float> job_apply_args<float>(const JobDesc& J) {
   A.g = J.G;
   A.pix = J.pix;
   A.cs = J.cs32;
+  A.ncs = J.nphase_total;
   A.hx = reinterpret_cast<float*>(J.hx);
   A.hy = reinterpret_cast<float*>(J.hy);
   A.hd = reinterpret_cast<float*>(J.hd);
   return A;
 }
 
-// Slots of the per-job partial array.
-enum : int { SL_A = 0, SL_B = 1, SL_C = 2, SL_U = 3, SL_GG = 4, SL_ZG = 5, SL_S = 6 /* 6..17 */ };
-constexpr int kJobSlots = 18;
 
 // FP64 K u into g (in-tile part + halos), all parts, then a job barrier.  The
 // apply arguments sit in shared memory (read there, not held in registers).
@@ -334,6 +340,7 @@ static __device__ void job_fold(const JobDesc& J, int part) {
 // writes them, every thread reads them after a barrier, so neither occupies
 // registers during the sweeps.
 static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engine_kernel(EngineArgs E) {
+  static_assert(sizeof(ApplySmem<float>) <= sizeof(ApplySmem<double>), "the FP32 tile shares the FP64 tile's memory");
   __shared__ __align__(16) unsigned char smraw[sizeof(ApplySmem<double>)];
   __shared__ double red[NT / 32];
   __shared__ int s_idx, s_part;
@@ -351,7 +358,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       const int idx = (int)atomicAdd(E.head, 1u);
       s_idx = idx;
       if (idx < E.nparts_total) {
-        sJ = E.jobs[E.part_job[idx]];
+        sJ = E.jobs[E3D_IDX(E.part_job[idx], E.njobs)];
         s_part = E.part_rank[idx];
       }
     }

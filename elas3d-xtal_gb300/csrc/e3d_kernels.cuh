@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <type_traits>
 
+#include "e3d_bounds.cuh"
 #include "e3d_device.cuh"
 #include "e3d_tma.cuh"
 
@@ -22,7 +23,7 @@ constexpr int TILE_Y = 8;
 
 // Tuning knobs of the persistent PCG kernel (set at build time).
 #ifndef E3D_PB_UNROLL_F32
-#define E3D_PB_UNROLL_F32 2  // phase-B nodes in flight per thread, FP32 form
+#define E3D_PB_UNROLL_F32 1  // phase-B nodes in flight per thread, FP32 form (2 spills under the 128-register cap)
 #endif
 #ifndef E3D_PB_UNROLL_F64
 #define E3D_PB_UNROLL_F64 1  // phase-B nodes in flight per thread, FP64 form
@@ -41,8 +42,20 @@ constexpr int TILE_Y = 8;
 #ifndef E3D_TMA_STAGES
 #define E3D_TMA_STAGES (E3D_RING_ZS + 4)  // ring stages per block (ZS + 1 in use, the rest in flight)
 #endif
+// FP32 tile state kept in shared memory instead of registers: the transformed
+// lower node plane (rebuilt from the node buffer for each element) and the
+// upper-plane forces carried to the next element (one slot per thread).  With
+// the first, the FP32 persistent kernel no longer spills under its 128-register
+// cap (500^3 inner iteration 6.9 ms, from 9.2); the second costs more shared
+// memory traffic than it saves (6.9 ms either way) and stays off.
+#ifndef E3D_F32_POLD_SMEM
+#define E3D_F32_POLD_SMEM 1
+#endif
+#ifndef E3D_F32_CARRY_SMEM
+#define E3D_F32_CARRY_SMEM 0
+#endif
 #ifndef E3D_PB_UNROLL_RING
-#define E3D_PB_UNROLL_RING (E3D_RING_ZS == 2 ? 4 : 2)  // phase-B nodes in flight per thread, ring kernel
+#define E3D_PB_UNROLL_RING (E3D_RING_ZS == 2 ? 4 : 1)  // phase-B nodes in flight per thread, ring kernel
 #endif
 constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
 
@@ -58,6 +71,9 @@ struct GridDims {
   int tz;             // element planes per tile
   long long ntiles;
 };
+
+// Length of one tile-edge halo buffer (hx, hy, hd) with w values per plane row.
+__host__ __device__ inline long long halo_len(const GridDims& G, int w) { return 3LL * G.ntiles * G.tz * w; }
 
 // Periodic wrap of v into [0, n); the callers pass neighbours (v in [-n, 2n)),
 // handled without an integer division.
@@ -91,6 +107,7 @@ struct ApplyArgs {
   GridDims g;
   const int32_t* __restrict__ pix;  // 0-based phase per voxel
   const T* __restrict__ cs;         // scaled stiffness table
+  int ncs;                          // rows of cs (every phase id is below it)
   const T* __restrict__ x;          // input (or h_old when fused)
   const T* __restrict__ zv;         // z (fused Fletcher-Reeves update only)
   T gamma;                          // FR coefficient
@@ -102,11 +119,19 @@ struct ApplyArgs {
   T* __restrict__ hd;               // [3][ntiles][tz]
 };
 
-template <typename T>
-struct ApplySmem {
+template <typename T, bool CARRY>
+struct ApplySmemT {
   T node[2][3][(TILE_X + 1) * (TILE_Y + 1)];
   T r[9][NT];
 };
+template <typename T>
+struct ApplySmemT<T, true> {
+  T node[2][3][(TILE_X + 1) * (TILE_Y + 1)];
+  T r[9][NT];
+  T carry[12][NT];
+};
+template <typename T>
+using ApplySmem = ApplySmemT<T, sizeof(T) == 4 && E3D_F32_CARRY_SMEM != 0>;
 
 // ---------------------------------------------------------------------------
 // TMA plane ring of the fused FP32 stencil.  One stage holds one node plane of
@@ -332,7 +357,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   auto prefetch = [&](int zl) {
     const int zp = wrapi(zl, G.nz);
     if (active) {
-      const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
+      const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * zp, ns);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         if (need_x) px_own[c] = __ldcg(A.x + m + c * ns);
@@ -340,7 +365,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       }
     }
     if (tid < nhalo) {
-      const long long m = (long long)hgx + (long long)G.nx * hgy + nxy * zp;
+      const long long m = E3D_IDX((long long)hgx + (long long)G.nx * hgy + nxy * zp, ns);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         if (need_x) px_h[c] = __ldcg(A.x + m + c * ns);
@@ -365,7 +390,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       T v[3];
       combine(pz_own, px_own, v);
       if (FUSED && own) {
-        const long long m = (long long)xg + (long long)G.nx * yg + nxy * zp;
+        const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * zp, ns);
 #pragma unroll
         for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = v[c];
       }
@@ -376,7 +401,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       T v[3];
       combine(pz_h, px_h, v);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) buf0[c * stride + hly * (TILE_X + 1) + hlx] = v[c];
+      for (int c = 0; c < 3; ++c) buf0[E3D_IDX(c * stride + hly * (TILE_X + 1) + hlx, 3 * stride)] = v[c];
     }
   };
   auto read_corners = [&](int zl, T (&v)[3][4]) {
@@ -392,6 +417,8 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
     }
   };
 
+  constexpr bool kPoldSmem = sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0;
+  constexpr bool kCarrySmem = sizeof(T) == 4 && E3D_F32_CARRY_SMEM != 0;
   T Pold[3][4], carry[3][4];
   // FP32: the tile's share of h.Ah is summed in FP32 and added to the FP64
   // accumulator once per tile; FP64: every node's term goes straight into it.
@@ -406,25 +433,31 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   prefetch(z0 - 1);
   commit(z0 - 1, false);
   __syncthreads();
-  if (active) {
+  if (!kPoldSmem && active) {
     T v0[3][4];
     read_corners(z0 - 1, v0);
 #pragma unroll
     for (int c = 0; c < 3; ++c) had_xy(v0[c], Pold[c]);
   }
   prefetch(z0);
-  int ph_cur = active ? __ldcs(A.pix + ecol + nxy * wrapi(z0 - 1, G.nz)) : 0;
+  int ph_cur = active ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(z0 - 1, G.nz), ns)) : 0;
   const int htiles_stride = G.tz;  // per-tile plane stride in halo buffers
   for (int k = z0 - 1; k < z0 + wz; ++k) {
     const bool own_next = (k + 1 >= z0) && (k + 1 < z0 + wz);
     commit(k + 1, own_next);
     __syncthreads();
     if (k + 2 <= z0 + wz) prefetch(k + 2);
-    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldcs(A.pix + ecol + nxy * wrapi(k + 1, G.nz)) : 0;
+    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(k + 1, G.nz), ns)) : 0;
     T rr[3][4];
     if (active) {
       T nxt[3][4];
       read_corners(k + 1, nxt);
+      if constexpr (kPoldSmem) {  // plane k, intact until the barrier that ends this step
+        T v0[3][4];
+        read_corners(k, v0);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) had_xy(v0[c], Pold[c]);
+      }
       T Pn[3][4];
       T h[3][8];
 #pragma unroll
@@ -438,9 +471,9 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       }
       T f[3][8];
       if constexpr (sizeof(T) == 4)
-        element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+        element_modal_f32(A.cs + E3D_IDX(ph_cur, A.ncs) * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
       else
-        element_modal<T>(A.cs + (long long)ph_cur * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
+        element_modal<T>(A.cs + E3D_IDX(ph_cur, A.ncs) * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         T lo[4];
@@ -448,12 +481,19 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         for (int b = 0; b < 4; ++b) {
           lo[b] = f[c][b] - f[c][b + 4];
           const T hi = f[c][b] + f[c][b + 4];
-          if (k >= z0) lo[b] += carry[c][b];
-          carry[c][b] = hi;
+          if constexpr (kCarrySmem) {
+            if (k >= z0) lo[b] += sm.carry[4 * c + b][tid];
+            sm.carry[4 * c + b][tid] = hi;
+          } else {
+            if (k >= z0) lo[b] += carry[c][b];
+            carry[c][b] = hi;
+          }
         }
         if (k >= z0) had_xy_adj(lo, rr[c]);
+        if constexpr (!kPoldSmem) {
 #pragma unroll
-        for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+          for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
+        }
       }
     }
     // plane k's values for the dot products, read before the barrier below
@@ -483,7 +523,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
       __syncthreads();
       if (active) {
         const int lz = k - z0;
-        const long long m = (long long)xg + (long long)G.nx * yg + nxy * wrapi(k, G.nz);
+        const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * wrapi(k, G.nz), ns);
         T hxv[3], hyv[3], acc[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -500,20 +540,22 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         const long long hb = tile * htiles_stride + lz;
         if (tx == wx - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty] = hxv[c];
+          for (int c = 0; c < 3; ++c) A.hx[E3D_IDX(((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty, halo_len(G, TILE_Y))] = hxv[c];
           add_dot(hk[0][1] * hxv[0] + hk[1][1] * hxv[1] + hk[2][1] * hxv[2]);
         }
         if (ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx] = hyv[c];
+          for (int c = 0; c < 3; ++c) A.hy[E3D_IDX(((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx, halo_len(G, TILE_X))] = hyv[c];
           add_dot(hk[0][2] * hyv[0] + hk[1][2] * hyv[1] + hk[2][2] * hyv[2]);
         }
         if (tx == wx - 1 && ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * htiles_stride + hb] = rr[c][3];
+          for (int c = 0; c < 3; ++c) A.hd[E3D_IDX((long long)c * G.ntiles * htiles_stride + hb, halo_len(G, 1))] = rr[c][3];
           add_dot(hk[0][3] * rr[0][3] + hk[1][3] * rr[1][3] + hk[2][3] * rr[2][3]);
         }
       }
+    } else if constexpr (kPoldSmem) {
+      __syncthreads();  // plane z0-1 was re-read: the next step refills its buffer
     }
     ph_cur = ph_nxt;
   }
@@ -577,8 +619,8 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
     }
   };
   auto hval = [&](const unsigned char* st, int off) -> float {
-    const float x = reinterpret_cast<const float*>(st)[off];
-    const float z = reinterpret_cast<const float*>(st + kRingVec)[off];
+    const float x = reinterpret_cast<const float*>(st)[E3D_IDX(off, kRingVec / 4)];
+    const float z = reinterpret_cast<const float*>(st + kRingVec)[E3D_IDX(off, kRingVec / 4)];
     return A.reset ? z : fmaf(A.gamma, x, z);
   };
   auto corners = [&](const unsigned char* st, float (&v)[3][4]) {
@@ -621,7 +663,7 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
           float nxt[3][4];
           corners(st1, nxt);
           if (kk + 1 >= z0 && kk + 1 < z0 + wz) {
-            const long long m = ncol + nxy * (kk + 1);
+            const long long m = E3D_IDX(ncol + nxy * (kk + 1), ns);
 #pragma unroll
             for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = nxt[c][0];
           }
@@ -637,7 +679,7 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
             }
           }
           float f[3][8];
-          element_modal_f32(A.cs + (long long)ph_cur * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
+          element_modal_f32(A.cs + E3D_IDX(ph_cur, A.ncs) * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             float lo[4];
@@ -686,7 +728,7 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
       if (j < ne && kk >= z0 && active) {
         const float(*r)[NT] = sm.r[step & 1] + 9 * j;
         const int lz = kk - z0;
-        const long long m = ncol + nxy * kk;
+        const long long m = E3D_IDX(ncol + nxy * kk, ns);
         float hxv[3], hyv[3], acc[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -702,17 +744,17 @@ static __device__ void apply_tile_ring(const ApplyArgs<float>& A, long long tile
         const long long hb = tile * hstride + lz;
         if (tx == wx - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hx[((long long)c * G.ntiles * hstride + hb) * TILE_Y + ty] = hxv[c];
+          for (int c = 0; c < 3; ++c) A.hx[E3D_IDX(((long long)c * G.ntiles * hstride + hb) * TILE_Y + ty, halo_len(G, TILE_Y))] = hxv[c];
           dot32 += hk[j][0][1] * hxv[0] + hk[j][1][1] * hxv[1] + hk[j][2][1] * hxv[2];
         }
         if (ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hy[((long long)c * G.ntiles * hstride + hb) * TILE_X + tx] = hyv[c];
+          for (int c = 0; c < 3; ++c) A.hy[E3D_IDX(((long long)c * G.ntiles * hstride + hb) * TILE_X + tx, halo_len(G, TILE_X))] = hyv[c];
           dot32 += hk[j][0][2] * hyv[0] + hk[j][1][2] * hyv[1] + hk[j][2][2] * hyv[2];
         }
         if (tx == wx - 1 && ty == wy - 1) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.hd[(long long)c * G.ntiles * hstride + hb] = rr[j][c][3];
+          for (int c = 0; c < 3; ++c) A.hd[E3D_IDX((long long)c * G.ntiles * hstride + hb, halo_len(G, 1))] = rr[j][c][3];
           dot32 += hk[j][0][3] * rr[j][0][3] + hk[j][1][3] * rr[j][1][3] + hk[j][2][3] * rr[j][2][3];
         }
       }
@@ -738,17 +780,17 @@ __device__ __forceinline__ void halo_add(const GridDims& G, const T* __restrict_
   if (lx == 0) {
     const long long t = (long long)txl + (long long)G.ntx * (tiy + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + (c * per_c + t * G.tz + lz) * TILE_Y + ly);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + E3D_IDX((c * per_c + t * G.tz + lz) * TILE_Y + ly, 3 * per_c * TILE_Y));
   }
   if (ly == 0) {
     const long long t = (long long)tix + (long long)G.ntx * (tyd + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + (c * per_c + t * G.tz + lz) * TILE_X + lx);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + E3D_IDX((c * per_c + t * G.tz + lz) * TILE_X + lx, 3 * per_c * TILE_X));
   }
   if (lx == 0 && ly == 0) {
     const long long t = (long long)txl + (long long)G.ntx * (tyd + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + c * per_c + t * G.tz + lz);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + E3D_IDX(c * per_c + t * G.tz + lz, 3 * per_c));
   }
 }
 
@@ -766,17 +808,17 @@ __device__ __forceinline__ void halo_add_tile(const GridDims& G, const T* __rest
   if (lx == 0) {
     const long long t = (long long)txl + (long long)G.ntx * (tiy + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + (c * per_c + t * G.tz + lz) * TILE_Y + ly);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hx + E3D_IDX((c * per_c + t * G.tz + lz) * TILE_Y + ly, 3 * per_c * TILE_Y));
   }
   if (ly == 0) {
     const long long t = (long long)tix + (long long)G.ntx * (tyd + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + (c * per_c + t * G.tz + lz) * TILE_X + lx);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hy + E3D_IDX((c * per_c + t * G.tz + lz) * TILE_X + lx, 3 * per_c * TILE_X));
   }
   if (lx == 0 && ly == 0) {
     const long long t = (long long)txl + (long long)G.ntx * (tyd + plane);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + c * per_c + t * G.tz + lz);
+    for (int c = 0; c < 3; ++c) v[c] += __ldcg(hd + E3D_IDX(c * per_c + t * G.tz + lz, 3 * per_c));
   }
 }
 
@@ -1054,7 +1096,7 @@ static __global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* _
       bool any;
       element_delta(G, J, ex, ey, ez, d, any);
       if (!any) continue;
-      const int ph = pix[(long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez];
+      const int ph = pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
       const double* D = dk + (long long)ph * 576;
       for (int i = 0; i < 3; ++i) {
         double s = 0.0;
@@ -1100,7 +1142,7 @@ static __global__ void __launch_bounds__(256) femat_c_kernel(GridDims G, JumpPar
     double d[8][3];
     bool any;
     element_delta(G, J, i, j, k, d, any);
-    const int ph = pix[(long long)i + (long long)G.nx * j + (long long)G.nx * G.ny * k];
+    const int ph = pix[E3D_IDX((long long)i + (long long)G.nx * j + (long long)G.nx * G.ny * k, G.ns)];
     const double* D = dk + (long long)ph * 576;
     double e = 0.0;
     for (int r = 0; r < 24; ++r) {
@@ -1179,7 +1221,7 @@ static __global__ void bjacobi_kernel(GridDims G, const int32_t* __restrict__ pi
     const int a = kRefToCorner[ra];
     const int ex = wrapi(x - (a & 1), G.nx), ey = wrapi(y - ((a >> 1) & 1), G.ny),
               ez = wrapi(z - ((a >> 2) & 1), G.nz);
-    const int ph = pix[(long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez];
+    const int ph = pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
     const double* D = dkd + (long long)ph * 72 + ra * 9;
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) M[i][j] = (ra == 0) ? D[i * 3 + j] : M[i][j] + D[i * 3 + j];
@@ -1213,7 +1255,7 @@ __device__ __forceinline__ void voxel_strain(const GridDims& G, const JumpParams
     const int ox = a & 1, oy = (a >> 1) & 1, oz = (a >> 2) & 1;
     const int xx = x + ox >= G.nx ? 0 : x + ox, yy = y + oy >= G.ny ? 0 : y + oy,
               zz = z + oz >= G.nz ? 0 : z + oz;
-    const long long mm = (long long)xx + (long long)G.nx * yy + (long long)G.nx * G.ny * zz;
+    const long long mm = E3D_IDX((long long)xx + (long long)G.nx * yy + (long long)G.nx * G.ny * zz, G.ns);
     for (int c = 0; c < 3; ++c) v[c][a] = u[mm + c * G.ns];
   }
   // periodic jump, x then y then z as at :2282-2323
@@ -1265,7 +1307,7 @@ static __global__ void __launch_bounds__(256) stress_avg_kernel(GridDims G, Jump
     const int ph = pix[m];
     for (int r = 0; r < 6; ++r) {
       double s = 0.0;
-      for (int c = 0; c < 6; ++c) s += cmod[ph + (long long)nphase * (r + 6 * c)] * eps[c];
+      for (int c = 0; c < 6; ++c) s += cmod[E3D_IDX(ph, nphase) + (long long)nphase * (r + 6 * c)] * eps[c];
       acc[r] += s;
       acc[6 + r] += eps[r];
     }
@@ -1289,7 +1331,7 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
   double s6[6];
   for (int r = 0; r < 6; ++r) {
     double s = 0.0;
-    for (int c = 0; c < 6; ++c) s += cmod[ph + (long long)nphase * (r + 6 * c)] * eps[c];
+    for (int c = 0; c < 6; ++c) s += cmod[E3D_IDX(ph, nphase) + (long long)nphase * (r + 6 * c)] * eps[c];
     s6[r] = s;
     if (sigma) sigma[m + r * G.ns] = s;
   }
@@ -1328,7 +1370,7 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
 #pragma unroll
       for (int j = 0; j < U; ++j) {
         if (lz0 + j < wz) {
-          const long long m = col + nxy * (z0 + lz0 + j);
+          const long long m = E3D_IDX(col + nxy * (z0 + lz0 + j), ns);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             ah[j][c] = __ldcg(Ah + m + c * ns);
@@ -1343,7 +1385,7 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
 #pragma unroll
       for (int j = 0; j < U; ++j) {
         if (lz0 + j < wz) {
-          const long long m = col + nxy * (z0 + lz0 + j);
+          const long long m = E3D_IDX(col + nxy * (z0 + lz0 + j), ns);
           halo_add_tile<T>(G, hx, hy, hd, tix, tiy, tiz, tx, ty, lz0 + j, ah[j]);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
@@ -1492,7 +1534,6 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
   if (s.status != PCG_RUNNING) return;
   const bool lead = threadIdx.x == 0;
   const GridDims& G = P.A.g;
-  const long long ns = G.ns;
   const int it_end = min(s.it + P.it_limit, s.max_iter);
   while (s.it < it_end) {
     // ---- phase A: fused direction update + stencil + h.Ah
@@ -1561,7 +1602,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
       } else {
         const double rel_res = sqrt(gg_new / s.gg0);
         s.rel_res = rel_res;
-        if (blockIdx.x == 0 && P.history) P.history[s.it - 1] = rel_res;
+        if (blockIdx.x == 0 && P.history) P.history[E3D_IDX(s.it - 1, s.max_iter)] = rel_res;
         if (s.divergence_reset && rel_res > 10.0 * s.rel_res_prev && s.it > 1) {  // :1961-1981
           s.reset = 1;
           s.resets += 1;
@@ -1703,7 +1744,7 @@ static __global__ void replace_scalars_kernel(const double* __restrict__ partial
       S.rel_res = rel;
       S.rel_res_prev = rel;
       if (!S.reset) S.gamma = gg / S.gglast;
-      if (history && S.it > 0) history[S.it - 1] = rel;
+      if (history && S.it > 0) history[E3D_IDX(S.it - 1, S.max_iter)] = rel;
       if (S.status == PCG_CONVERGED && !(rel < S.tol)) S.status = PCG_RUNNING;
       if (S.status == PCG_RUNNING && rel < S.tol) S.status = PCG_CONVERGED;
     }

@@ -180,6 +180,7 @@ extern "C" int32_t e3d_apply_noalloc(int32_t nx, int32_t ny, int32_t nz, int32_t
   A.g = G;
   A.pix = d_pix;  // 1-based ids index the table (row 0 unused)
   A.cs = table;
+  A.ncs = nphase + 1;
   A.x = d_x;
   A.y = d_y;
   A.hx = hx;
@@ -191,3 +192,6 @@ extern "C" int32_t e3d_apply_noalloc(int32_t nx, int32_t ny, int32_t nz, int32_t
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail("cudaStreamSynchronize", e);
   return E3D_OK;
 }
+
+// Bounds-checked build: this translation unit's record (read by e3d_debug_bounds).
+int e3d_bounds_take_noalloc(long long out[4]) { return e3d_noalloc_tu::e3d::bounds_take(out); }

@@ -200,9 +200,10 @@ int64_t e3d_device_bytes(const e3d_handle_t* h);
 int64_t e3d_launch_count(const e3d_handle_t* h);
 
 /* Which inner stencil the solve runs: E3D_PATH_FP64 (plain FP64 form),
- * E3D_PATH_F32 (mixed form, per-thread loads) or E3D_PATH_F32_TMA (mixed form,
- * node planes staged in shared memory by TMA; grids with nx % 4 == 0 unless
- * the environment sets E3D_NO_TMA=1 when the handle is created). */
+ * E3D_PATH_F32 (mixed form, per-thread loads: the default) or
+ * E3D_PATH_F32_TMA (mixed form, node planes staged in shared memory by TMA;
+ * when the environment sets E3D_TMA=1 as the handle is created and
+ * nx % 4 == 0). */
 enum { E3D_PATH_FP64 = 0, E3D_PATH_F32 = 1, E3D_PATH_F32_TMA = 2 };
 int32_t e3d_stencil_path(const e3d_handle_t* h);
 
@@ -241,6 +242,25 @@ int32_t e3d_probe_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops
  * E3D_ERR_TIMEOUT when the wait ran out and was reported through the error flag
  * (the context stays usable), any other status otherwise. */
 int32_t e3d_selftest_timeout(int32_t device, int32_t which, double timeout_s);
+
+/* Bounds-checked debug build (no counterpart in the reference; the library
+ * compiled with -DE3D_BOUNDS, build recipe option bounds=True): reads and
+ * clears the record of the indices that the checked kernels found outside
+ * their buffers since the last call, on the current device.  report = {count,
+ * unit, line, index, limit}: the number of such indices (0 in a clean run)
+ * and, for the first one, the translation unit (0 solver, 1 batch and serve
+ * engine, 2 allocation-free apply), the source line of the check, the index
+ * and the buffer's length.  A checked kernel uses element 0 in place of a bad
+ * index, so nothing is read or written outside a buffer.  Returns
+ * E3D_ERR_STATE (report zeroed) in a library built without the checks. */
+int32_t e3d_debug_bounds(int64_t report[5]);
+
+/* Test hook of the checked build: one kernel hands the check an index past
+ * the end of its 32-element buffer, which must be counted and redirected to
+ * element 0.  Clears the record first.  Returns E3D_OK when e3d_debug_bounds
+ * then reports exactly that index, E3D_ERR_STATE in a library built without
+ * the checks (no kernel runs there). */
+int32_t e3d_selftest_bounds(int32_t device);
 
 const char* e3d_strerror(int32_t status);
 /* Text of the last CUDA error seen by any handle in this thread. */

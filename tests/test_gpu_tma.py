@@ -35,11 +35,11 @@ def _case(nx, ny, nz, ngrains, seed):
     return p, pix, rod
 
 
-def _solve(p, pix, rod, no_tma, monkeypatch):
-    if no_tma:
-        monkeypatch.setenv("E3D_NO_TMA", "1")
+def _solve(p, pix, rod, tma, monkeypatch):
+    if tma:
+        monkeypatch.setenv("E3D_TMA", "1")
     else:
-        monkeypatch.delenv("E3D_NO_TMA", raising=False)
+        monkeypatch.delenv("E3D_TMA", raising=False)
     with e3d.Elas3D(p) as g:
         path = g.stencil_path()
         g.upload(pix, rod)
@@ -65,8 +65,8 @@ SHAPES = [
 @pytest.mark.parametrize("shape", SHAPES)
 def test_tma_stencil_matches_per_thread_loads(shape, monkeypatch):
     p, pix, rod = _case(*shape, seed=sum(shape))
-    path_t, rt, ut = _solve(p, pix, rod, False, monkeypatch)
-    path_r, rr, ur = _solve(p, pix, rod, True, monkeypatch)
+    path_t, rt, ut = _solve(p, pix, rod, True, monkeypatch)
+    path_r, rr, ur = _solve(p, pix, rod, False, monkeypatch)
     assert path_t == "f32_tma" and path_r == "f32"
     assert rt["exit_reason"] == e3d.EXIT_CONVERGED and rr["exit_reason"] == e3d.EXIT_CONVERGED
     assert abs(rt["iterations"] - rr["iterations"]) <= 1
@@ -78,7 +78,7 @@ def test_tma_stencil_matches_per_thread_loads(shape, monkeypatch):
 
 def test_unaligned_rows_keep_per_thread_loads(monkeypatch):
     p, pix, rod = _case(30, 8, 8, 4, seed=3)  # 30 * 4 bytes is not a multiple of 16
-    path, res, _ = _solve(p, pix, rod, False, monkeypatch)
+    path, res, _ = _solve(p, pix, rod, True, monkeypatch)
     assert path == "f32"
     assert res["exit_reason"] == e3d.EXIT_CONVERGED
 
