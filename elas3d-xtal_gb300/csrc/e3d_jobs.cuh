@@ -290,7 +290,10 @@ static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part
 // One FP32 inner iteration's two sweeps, each kept out of line so that it gets
 // its own register allocation rather than the engine kernel's.
 // Fused direction update + stencil: returns this part's h.Ah.
-static __device__ __noinline__ double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
+#ifndef E3D_ENGINE_SWEEP_ATTR
+#define E3D_ENGINE_SWEEP_ATTR __noinline__
+#endif
+static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
                                                      ApplySmem<float>& sm) {
   __shared__ ApplyArgs<float> sA;
   if (threadIdx.x == 0) {

@@ -320,7 +320,7 @@ __device__ __forceinline__ void ring_drain(PlaneRing& R) {
 // iteration (src/elas3dxtal_pcg.f90:1988-1995) folded into this pass -- and
 // h_new is stored for the tile's own nodes.  Returns this thread's share of
 // h_new . (K h_new) through hAh.
-template <typename T, bool FUSED>
+template <typename T, bool FUSED, bool POLD_SMEM = (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0)>
 __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& sm, double& hAh) {
   const GridDims& G = A.g;
   const int tid = threadIdx.x;
@@ -417,7 +417,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
     }
   };
 
-  constexpr bool kPoldSmem = sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0;
+  constexpr bool kPoldSmem = POLD_SMEM;
   constexpr bool kCarrySmem = sizeof(T) == 4 && E3D_F32_CARRY_SMEM != 0;
   T Pold[3][4], carry[3][4];
   // FP32: the tile's share of h.Ah is summed in FP32 and added to the FP64
