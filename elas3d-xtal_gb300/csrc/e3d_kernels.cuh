@@ -54,6 +54,13 @@ constexpr int TILE_Y = 8;
 #ifndef E3D_F32_CARRY_SMEM
 #define E3D_F32_CARRY_SMEM 0
 #endif
+// FP32 persistent kernel (per-thread loads): the correction update du -= lam*h
+// of iteration k is applied in phase A of iteration k+1, which loads h there
+// anyway, so phase B reads neither h nor du; the update still pending when the
+// launch ends is applied before it returns.
+#ifndef E3D_F32_DEFER_U
+#define E3D_F32_DEFER_U 1
+#endif
 #ifndef E3D_PB_UNROLL_RING
 #define E3D_PB_UNROLL_RING (E3D_RING_ZS == 2 ? 4 : 1)  // phase-B nodes in flight per thread, ring kernel
 #endif
@@ -117,6 +124,8 @@ struct ApplyArgs {
   T* __restrict__ hx;               // [3][ntiles][tz][TILE_Y]
   T* __restrict__ hy;               // [3][ntiles][tz][TILE_X]
   T* __restrict__ hd;               // [3][ntiles][tz]
+  T* __restrict__ du;               // deferred correction update (DEFER_U): du -= lam_prev * x, own nodes
+  T lam_prev;
 };
 
 template <typename T, bool CARRY>
@@ -320,7 +329,7 @@ __device__ __forceinline__ void ring_drain(PlaneRing& R) {
 // iteration (src/elas3dxtal_pcg.f90:1988-1995) folded into this pass -- and
 // h_new is stored for the tile's own nodes.  Returns this thread's share of
 // h_new . (K h_new) through hAh.
-template <typename T, bool FUSED, bool POLD_SMEM = (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0)>
+template <typename T, bool FUSED, bool POLD_SMEM = (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), bool DEFER_U = false>
 __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& sm, double& hAh) {
   const GridDims& G = A.g;
   const int tid = threadIdx.x;
@@ -352,16 +361,18 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   // Raw loads of one node plane are issued a step ahead (prefetch) so they are
   // in flight while the previous element computes; commit forms h_new and
   // stores the plane into shared memory.
-  T pz_own[3], px_own[3], pz_h[3], px_h[3];
+  T pz_own[3], px_own[3], pz_h[3], px_h[3], pu_own[3];
   const bool need_x = !FUSED || !A.reset;
   auto prefetch = [&](int zl) {
     const int zp = wrapi(zl, G.nz);
     if (active) {
       const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * zp, ns);
+      const bool own = zl >= z0 && zl < z0 + wz;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        if (need_x) px_own[c] = __ldcg(A.x + m + c * ns);
+        if (need_x || (DEFER_U && own)) px_own[c] = __ldcg(A.x + m + c * ns);
         if (FUSED) pz_own[c] = __ldcg(A.zv + m + c * ns);
+        if (DEFER_U && own) pu_own[c] = A.du[m + c * ns];
       }
     }
     if (tid < nhalo) {
@@ -393,6 +404,10 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * zp, ns);
 #pragma unroll
         for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = v[c];
+        if constexpr (DEFER_U) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) A.du[m + c * ns] = pu_own[c] - A.lam_prev * px_own[c];
+        }
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) buf0[c * stride + ty * (TILE_X + 1) + tx] = v[c];
@@ -1346,7 +1361,7 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
 // loads are in flight: u -= lam h, g -= lam Ah (+ tile-edge halos),
 // z = Minv g (src/elas3dxtal_pcg.f90:1913-1932, symmetric Minv); returns this
 // thread's share of z.g (FP32: summed per tile column in FP32, then in FP64).
-template <typename T, int U = (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64)>
+template <typename T, int U = (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64), bool UPD_U = true>
 __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long first, long long stride, T lam,
                                                    const T* __restrict__ hc, const T* __restrict__ Ah,
                                                    const T* __restrict__ hx, const T* __restrict__ hy,
@@ -1374,8 +1389,10 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             ah[j][c] = __ldcg(Ah + m + c * ns);
-            hv[j][c] = __ldcg(hc + m + c * ns);
-            uv[j][c] = u[m + c * ns];
+            if constexpr (UPD_U) {
+              hv[j][c] = __ldcg(hc + m + c * ns);
+              uv[j][c] = u[m + c * ns];
+            }
             gv[j][c] = g[m + c * ns];
           }
 #pragma unroll
@@ -1389,7 +1406,7 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
           halo_add_tile<T>(G, hx, hy, hd, tix, tiy, tiz, tx, ty, lz0 + j, ah[j]);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            u[m + c * ns] = uv[j][c] - lam * hv[j][c];
+            if constexpr (UPD_U) u[m + c * ns] = uv[j][c] - lam * hv[j][c];
             gv[j][c] = gv[j][c] - lam * ah[j][c];
             g[m + c * ns] = gv[j][c];
           }
@@ -1409,6 +1426,30 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
     if constexpr (sizeof(T) == 4) zg_t += (double)zg32;
   }
   return zg_t;
+}
+
+// u -= lam h over the owned nodes of tiles first, first + stride, ... (the same
+// tile and column ownership as apply_tile and pcg_update_tiles).
+template <typename T>
+__device__ void flush_u_tiles(const GridDims& G, long long first, long long stride, T lam, const T* __restrict__ h,
+                              T* __restrict__ u) {
+  const long long ns = G.ns;
+  const int tx = threadIdx.x % TILE_X, ty = threadIdx.x / TILE_X;
+  const long long nxy = (long long)G.nx * G.ny;
+  for (long long t = first; t < G.ntiles; t += stride) {
+    const int tix = (int)(t % G.ntx);
+    const int tiy = (int)((t / G.ntx) % G.nty);
+    const int tiz = (int)(t / ((long long)G.ntx * G.nty));
+    const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+    const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+    if (tx >= wx || ty >= wy) continue;
+    const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+    for (int lz = 0; lz < wz; ++lz) {
+      const long long m = E3D_IDX(col + nxy * (z0 + lz), ns);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) u[m + c * ns] = u[m + c * ns] - lam * __ldcg(h + m + c * ns);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1535,6 +1576,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
   const bool lead = threadIdx.x == 0;
   const GridDims& G = P.A.g;
   const int it_end = min(s.it + P.it_limit, s.max_iter);
+  constexpr bool kDeferU = sizeof(T) == 4 && !TMA && E3D_F32_DEFER_U != 0;
+  T lam_pending = T(0);  // kDeferU: du -= lam_pending * h_pending not yet applied
+  const T* h_pending = nullptr;
   while (s.it < it_end) {
     // ---- phase A: fused direction update + stencil + h.Ah
     ApplyArgs<T> A = P.A;
@@ -1545,13 +1589,17 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
     A.y = P.Ah;
     A.gamma = (T)s.gamma;
     A.reset = s.reset;
+    if constexpr (kDeferU) {
+      A.du = P.u;
+      A.lam_prev = lam_pending;
+    }
     double hAh_t = 0.0;
     if constexpr (TMA) ring_begin(ring, G, cur ? P.maps->h1 : P.maps->h0, blockIdx.x, gridDim.x, G.ntiles);
     for (long long t = blockIdx.x; t < G.ntiles; t += gridDim.x) {
       if constexpr (TMA)
         apply_tile_ring<E3D_RING_ZS>(A, t, sm, hAh_t, ring);
       else
-        apply_tile<T, true>(A, t, sm, hAh_t);
+        apply_tile<T, true, (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), kDeferU>(A, t, sm, hAh_t);
       __syncthreads();
     }
     {
@@ -1563,6 +1611,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
       if (lead) s.status = PCG_TIMEOUT;
       break;
     }
+    lam_pending = T(0);  // applied by this phase A
     const double hAh = reduce_broadcast(P.partA, gridDim.x, red);
     if (lead) {
       s.it += 1;
@@ -1581,8 +1630,12 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
     // (no index division), z unrolled so several nodes' loads are in flight.
     const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
     constexpr int U = TMA ? E3D_PB_UNROLL_RING : (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64);
-    const double zg_t = pcg_update_tiles<T, U>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy, P.A.hd,
-                                               P.minv, P.u, P.g, P.z);
+    const double zg_t = pcg_update_tiles<T, U, !kDeferU>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy,
+                                                         P.A.hd, P.minv, P.u, P.g, P.z);
+    if constexpr (kDeferU) {
+      lam_pending = lam;
+      h_pending = hc;
+    }
     {
       const double bs = block_sum<NT>(zg_t, red);
       if (threadIdx.x == 0) P.partB[blockIdx.x] = bs;
@@ -1619,6 +1672,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
   }
   __syncthreads();
   if (lead && s.status == PCG_RUNNING && s.it >= s.max_iter) s.status = PCG_MAXITER;
+  // The last update is applied by the threads whose phase A wrote those du and
+  // h values (same tile and column ownership), so no barrier is needed.
+  if constexpr (kDeferU)
+    if (lam_pending != T(0)) flush_u_tiles<T>(G, blockIdx.x, gridDim.x, lam_pending, h_pending, P.u);
   if constexpr (TMA) ring_drain(ring);
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.st = s;
 }
