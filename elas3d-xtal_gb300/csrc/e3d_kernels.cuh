@@ -405,8 +405,12 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
 #pragma unroll
         for (int c = 0; c < 3; ++c) A.hnew[m + c * ns] = v[c];
         if constexpr (DEFER_U) {
+          // nothing pending at the first step of a launch (lam_prev = 0): h_old
+          // may then hold another solve's direction and is not used
+          if (A.lam_prev != T(0)) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) A.du[m + c * ns] = pu_own[c] - A.lam_prev * px_own[c];
+            for (int c = 0; c < 3; ++c) A.du[m + c * ns] = pu_own[c] - A.lam_prev * px_own[c];
+          }
         }
       }
 #pragma unroll
