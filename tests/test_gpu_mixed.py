@@ -74,3 +74,35 @@ def test_mixed_iterate_split_equals_solve():
     assert abs(st["iterations"] - ra["iterations"]) <= 3
     ub, ua = b.get_u(), a.get_u()
     assert _rel(ub, ua) < 1e-6
+
+
+def test_handle_reused_after_breakdown_ignores_stale_directions():
+    """A solve that breaks down (NaN displacement) leaves NaN in the FP32
+    search-direction buffers; the next solve on the same handle must not use
+    them (the correction update deferred to the next stencil pass has nothing
+    pending at a solve's first step) and must equal a fresh handle's solve."""
+    p, pix, rod = W.c2(n=20)
+    p.precision = e3d.PREC_MIXED
+    p.refine_every = 20
+
+    def solve(g):
+        g.init_affine()
+        g.energy()
+        r = g.dembx()
+        return r, g.get_u()
+
+    with e3d.Elas3D(p) as g:
+        g.upload(pix, rod).femat()
+        g.set_u(np.full(3 * p.ns, np.nan))
+        with pytest.raises(e3d.E3DError):
+            g.energy()
+            g.solve_begin()
+            g.iterate(10)
+        r2, u2 = solve(g)
+    with e3d.Elas3D(p) as f:
+        f.upload(pix, rod).femat()
+        r1, u1 = solve(f)
+    assert r1["exit_reason"] == e3d.EXIT_CONVERGED
+    assert r2["exit_reason"] == e3d.EXIT_CONVERGED
+    assert r2["iterations"] == r1["iterations"]
+    assert np.array_equal(u1, u2)
