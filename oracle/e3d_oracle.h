@@ -2,8 +2,8 @@
  * e3d_oracle.h -- CPU oracle for the ELAS3D-Xtal voxel-FE PCG solve.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C/OpenMP restatement of the
- * reference's algorithm (src/elas3dxtal_pcg.f90) used as the checker for the
- * CUDA library and as the timed CPU baseline.  Nothing in the product library
+ * reference's algorithm (src/elas3dxtal_pcg.f90) that the tests compare the
+ * CUDA library against, and the timed CPU baseline.  Nothing in the product library
  * links, loads or calls it.
  *
  * Parity status: UNPINNED by reference outputs.  The reference ships no tests,

@@ -1,6 +1,6 @@
 """Mixed precision (E3D_PREC_MIXED): FP32 stencil + FP32 block-Jacobi inside an
 FP64 residual-replacement loop.  Results are compared with the FP64 oracle:
-energy within 1e-8 relative (the spec bar for this form), averaged
+energy within 1e-8 relative (the accuracy bar of this form), averaged
 stress within 1e-7, and the recomputed true residual meets the criterion."""
 import numpy as np
 import pytest
