@@ -738,10 +738,14 @@ int32_t e3d_serve_submit(e3d_server_t* s, const e3d_rve_t* rve, const double str
   if (!s || !rve || !strain || !rve->pix || !rve->rodrigues || rve->nx < 1 || rve->ny < 1 || rve->nz < 1 ||
       rve->ngrains < 1)
     return E3D_ERR_INPUT;
+  const long long ns = (long long)rve->nx * rve->ny * rve->nz;
+  // the phase-id range check of ppixel_hdf5 (src/elas3dxtal_pcg.f90:2986-2989),
+  // at submission so that a bad request is refused before it takes a slot
+  for (long long m = 0; m < ns; ++m)
+    if (rve->pix[m] < 1 || rve->pix[m] > rve->ngrains + 1) return E3D_ERR_INPUT;
   ServeJob* j = new ServeJob();
   j->id = s->next_id++;
   j->rve = *rve;
-  const long long ns = (long long)rve->nx * rve->ny * rve->nz;
   j->pix.assign(rve->pix, rve->pix + ns);
   j->rod.assign(rve->rodrigues, rve->rodrigues + 3 * (size_t)rve->ngrains);
   j->rve.pix = j->pix.data();

@@ -103,7 +103,9 @@ void e3d_serve_opts_defaults(e3d_serve_opts_t* o);
 int32_t e3d_serve_create(e3d_server_t** s, const e3d_serve_opts_t* opts);
 
 /* Queues one request: an RVE under a macro strain (tensor exx eyy ezz exz eyz
- * exy).  Inputs are copied; returns the request id through *id. */
+ * exy).  Inputs are copied; returns the request id through *id.  Phase ids
+ * outside [1, ngrains + 1] are refused with E3D_ERR_INPUT, and a request larger
+ * than the HBM budget with E3D_ERR_OOM. */
 int32_t e3d_serve_submit(e3d_server_t* s, const e3d_rve_t* rve, const double strain[6], int64_t* id);
 
 /* One scheduling round: admits queued requests while slots and HBM allow,

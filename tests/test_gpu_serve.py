@@ -98,3 +98,17 @@ def test_serve_cancel_queued_and_active_requests():
         ref = _oracle(*reqs[k])
         assert abs(out[k]["utot"] - ref["utot"]) <= ENERGY_TOL * abs(ref["utot"])
     assert now == 0
+
+
+def test_serve_refuses_bad_phase_ids_at_submission():
+    reqs = _requests()
+    rve, strain = reqs[2]
+    bad = dict(rve)
+    bad["pix"] = rve["pix"].copy()
+    bad["pix"][5] = rve["ngrains"] + 2  # one past the pore phase
+    with e3d.Server(round_iters=5, max_active=2) as srv:
+        with pytest.raises(e3d.E3DError):
+            srv.submit(bad, strain)
+        rid = srv.submit(rve, strain)  # the server is unaffected
+        out = _drain(srv, [rid])
+    assert out[0]["status"] == e3d.EXIT_CONVERGED
