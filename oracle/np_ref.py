@@ -206,15 +206,20 @@ class SparseModel:
         del D
         return inv
 
-    def pcg(self, tol=1e-8, maxit=10000, criterion=0, reset=True):
-        """The reference's PCG (src/elas3dxtal_pcg.f90:1527-2012) in numpy."""
+    def pcg(self, tol=1e-8, maxit=10000, criterion=0, reset=True, plain=False):
+        """The reference's PCG (src/elas3dxtal_pcg.f90:1527-2012) in numpy.
+        plain=True: the unpreconditioned CG of the serial and cg variants
+        (applications/sec3_1/serial/n_100x100x100/elas3dxtal_serial.f90:898-1052):
+        z = g, so gg = g.g and h starts as g."""
         ns = self.ns
         u = self.affine()
         g, _ = self.energy(u)
         gg0 = g @ g
-        Mi = self.block_jacobi()
+        Mi = None if plain else self.block_jacobi()
 
         def prec(v):
+            if plain:
+                return v.copy()
             V = v.reshape(3, ns).T
             return np.einsum("mij,mj->mi", Mi, V).T.ravel()
 

@@ -154,6 +154,24 @@ def test_solve_matches_independent_pcg():
     assert abs(r["utot"] - U) <= 1e-9 * abs(U)
 
 
+def test_plain_cg_matches_independent_cg():
+    """The oracle's identity-preconditioner mode is the unpreconditioned CG of
+    the reference's serial and cg variants (no divergence reset there)."""
+    p, pix, rod, s = _rand_problem(6, 5, 7, 4, seed=23, strain=[0, 0, 0, 5e-4, 0, 0])
+    p.precond = 1
+    p.divergence_reset = 0
+    r = O.run(p, pix, rod)
+    o = O.Oracle(p, pix, rod).femat()
+    sm = R.SparseModel(p.nx, p.ny, p.nz, pix, o.cmod_array(), s)
+    u, L = sm.pcg(tol=p.tol, reset=False, plain=True)
+    assert abs(r["lstep"] - L) <= 2
+    _, U = sm.energy(u)
+    assert abs(r["utot"] - U) <= 1e-9 * abs(U)
+    # and it takes more iterations than the block-Jacobi PCG on the same problem
+    p.precond = 0
+    assert O.run(p, pix, rod)["lstep"] < r["lstep"]
+
+
 def test_effective_modulus_between_voigt_and_reuss():
     rng = np.random.default_rng(8)
     ng, n = 6, 8
