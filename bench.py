@@ -224,12 +224,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     p, pix, rod = _workload(args.n)
-    # one warm-up iteration, then as many of the requested iterations as fit in
-    # about 90 s of CPU work (one 500^3 oracle iteration takes seconds)
-    warm = min(args.warmup, 1) if args.warmup > 0 else 1
+    # at most one warm-up iteration, which also sizes the timed sample: as many
+    # of the requested iterations as fit in about 90 s of CPU work (one 500^3
+    # oracle iteration takes seconds); without a warm-up all are timed
+    warm = min(args.warmup, 1)
     rate, cores, dt, done = cpu_oracle_rate(p, pix, rod, warm, args.steps, budget_s=90.0)
     sample = (f"{done} of the {args.steps} requested PCG iterations of the {args.n}^3 workload (capped at about "
-              f"90 s of CPU work) after {warm} warm-up iteration; each dembx call includes its block-Jacobi "
+              f"90 s of CPU work) after {warm} warm-up iteration(s); each dembx call includes its block-Jacobi "
               f"build, as in the reference")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws,
