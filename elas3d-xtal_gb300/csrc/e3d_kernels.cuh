@@ -1361,10 +1361,12 @@ static __global__ void stress_field_kernel(GridDims G, JumpParams J, const int32
 }
 
 // Phase B of a PCG iteration over tiles first, first + stride, ... < ntiles,
-// node loop in tile order (no index division), z unrolled so several nodes'
-// loads are in flight: u -= lam h, g -= lam Ah (+ tile-edge halos),
-// z = Minv g (src/elas3dxtal_pcg.f90:1913-1932, symmetric Minv); returns this
-// thread's share of z.g (FP32: summed per tile column in FP32, then in FP64).
+// node loop in tile order (no index division), U nodes of a column per thread
+// in flight (the defaults keep one: more spill under the register cap):
+// u -= lam h (unless UPD_U is false: the FP32 persistent kernel applies it in
+// the next phase A), g -= lam Ah (+ tile-edge halos), z = Minv g
+// (src/elas3dxtal_pcg.f90:1913-1932, symmetric Minv); returns this thread's
+// share of z.g (FP32: summed per tile column in FP32, then in FP64).
 template <typename T, int U = (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64), bool UPD_U = true>
 __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long first, long long stride, T lam,
                                                    const T* __restrict__ hc, const T* __restrict__ Ah,
@@ -1464,6 +1466,7 @@ __device__ void flush_u_tiles(const GridDims& G, long long first, long long stri
 //   A: h_new = z + gamma*h_old (or z), Ah = K h_new, partial h.Ah   | barrier
 //      lambda = gg/hAh (guards :1899-1907)
 //   B: u -= lambda h ; g -= lambda Ah ; z = Minv g ; partial z.g     | barrier
+//      (FP32 per-thread-load form: u -= lambda h moves into the next A)
 //      rel_res, divergence reset (:1961-1981), gamma (:1988), stop test (:2007)
 struct PcgState {
   double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
@@ -1631,7 +1634,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
     const double lambda = s.gg / hAh;
     const T lam = (T)lambda;
     // ---- phase B: u, g update, preconditioner, z.g -- node loop in tile order
-    // (no index division), z unrolled so several nodes' loads are in flight.
+    // (no index division); with kDeferU the u update waits for the next phase A.
     const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
     constexpr int U = TMA ? E3D_PB_UNROLL_RING : (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64);
     const double zg_t = pcg_update_tiles<T, U, !kDeferU>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy,
