@@ -172,6 +172,43 @@ def test_plain_cg_matches_independent_cg():
     assert O.run(p, pix, rod)["lstep"] < r["lstep"]
 
 
+# Cubic constants (GPa) of the reference's Zener-ratio sweep, keyed by the ratio
+# A = 2 C44 / (C11 - C12) that names each case
+# (applications/sec3_2/A_*/elas3dxtal_pcg.f90:68-70).
+A_SWEEP = {
+    0.5: (300.04, 84.95, 53.77), 0.75: (274.65, 97.64, 66.38), 1.0: (256.75, 106.59, 75.08),
+    1.5: (232.07, 118.93, 84.85), 2.0: (216.52, 126.70, 89.82), 3.0: (198.66, 135.64, 94.53),
+    4.0: (188.74, 140.60, 96.28), 5.0: (182.38, 143.78, 96.50),
+}
+
+
+@pytest.mark.parametrize("A", sorted(A_SWEEP))
+def test_zener_sweep_solves_match_independent_pcg(A):
+    """The oracle on the reference's own parameter sets: solves match the
+    independent scipy PCG (iterations within 2, energy within 1e-9), and a
+    single grain under a uniform strain carries <sigma> = cmod eps exactly."""
+    c11, c12, c44 = (v * 1e9 for v in A_SWEEP[A])
+    assert abs(2.0 * c44 / (c11 - c12) - A) < 1e-3 * A
+    p, pix, rod, s = _rand_problem(5, 6, 4, 3, seed=40 + int(10 * A), strain=[1e-3, 0, 0, 0, 5e-4, 0],
+                                   c11=c11, c12=c12, c44=c44)
+    r = O.run(p, pix, rod)
+    o = O.Oracle(p, pix, rod).femat()
+    sm = R.SparseModel(p.nx, p.ny, p.nz, pix, o.cmod_array(), s)
+    u, L = sm.pcg(tol=p.tol)
+    assert abs(r["lstep"] - L) <= 2
+    _, U = sm.energy(u)
+    assert abs(r["utot"] - U) <= 1e-9 * abs(U)
+    # one grain (no pores): the affine field is the solution and <sigma> = cmod eps,
+    # eps in engineering shear (tensor shear inputs doubled)
+    q, pix1, rod1, s1 = _rand_problem(4, 4, 4, 1, seed=7, pores=False, strain=[2e-4, -1e-4, 3e-4, 1e-4, 0, 2e-4],
+                                      c11=c11, c12=c12, c44=c44)
+    r1 = O.run(q, pix1, rod1)
+    eng = s1 * np.array([1, 1, 1, 2, 2, 2])
+    assert _rel(r1["epsav"], eng) < 1e-12
+    cm = O.Oracle(q, pix1, rod1).femat().cmod_array()[0]
+    assert _rel(r1["strav"], cm @ eng) < 1e-9
+
+
 def test_effective_modulus_between_voigt_and_reuss():
     rng = np.random.default_rng(8)
     ng, n = 6, 8
