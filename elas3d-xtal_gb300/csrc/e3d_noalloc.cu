@@ -16,7 +16,9 @@
 // the previous call's contents in it: the error flag is cleared on each call and
 // the table and halos are fully rewritten before they are read.  Calls that
 // overlap on the GPU (other streams, other host threads, same device) race on
-// the array and must be serialised by the caller.
+// the array and must be serialised by the caller.  Each call reads the
+// phase-check flag back into host memory and waits for its stream twice, so it
+// returns only once y is complete.  x and y must not overlap.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -101,15 +103,15 @@ GridDims noalloc_dims(int nx, int ny, int nz, int num_sms) {
   G.ny = ny;
   G.nz = nz;
   G.ns = (long long)nx * ny * nz;
-  G.ntx = (nx + TILE_X - 1) / TILE_X;
-  G.nty = (ny + TILE_Y - 1) / TILE_Y;
+  G.ntx = (int)(((long long)nx + TILE_X - 1) / TILE_X);
+  G.nty = (int)(((long long)ny + TILE_Y - 1) / TILE_Y);
   const long long cols = (long long)G.ntx * G.nty;
   const long long want = (long long)(num_sms > 0 ? num_sms : 1) * 4;
   const int ntz = (int)(want > cols ? std::min<long long>(nz, (want + cols - 1) / cols) : 1);
-  int tz = (nz + ntz - 1) / ntz;
+  int tz = (int)(((long long)nz + ntz - 1) / ntz);
   if (tz < 16) tz = std::min(nz, 16);
   G.tz = tz;
-  G.ntz = (nz + tz - 1) / tz;
+  G.ntz = (int)(((long long)nz + tz - 1) / tz);
   G.ntiles = cols * G.ntz;
   return G;
 }
@@ -124,11 +126,47 @@ long long scratch_doubles(const GridDims& G, int nphase) {
 
 extern "C" int32_t e3d_apply_noalloc(int32_t nx, int32_t ny, int32_t nz, int32_t nphase, const int32_t* d_pix,
                                      const double* d_cmod, const double* d_x, double* d_y, void* stream) {
-  if (!d_pix || !d_cmod || !d_x || !d_y || nx < 1 || ny < 1 || nz < 1 || nphase < 1) return E3D_ERR_INPUT;
+  if (!d_pix || !d_cmod || !d_x || !d_y) {
+    e3d_record_error_text("e3d_apply_noalloc: d_pix, d_cmod, d_x and d_y must not be NULL");
+    return E3D_ERR_INPUT;
+  }
+  if (nx < 1 || ny < 1 || nz < 1 || nphase < 1) {
+    e3d_record_error_text("e3d_apply_noalloc: nx, ny, nz and nphase must be at least 1");
+    return E3D_ERR_INPUT;
+  }
+  // The halos alone take 3*(TILE_X+TILE_Y+1)/(TILE_X*TILE_Y) > 1/4 double per
+  // node, so a grid above 4*kScratchDoubles nodes can never fit; refusing it
+  // here keeps every size computed below within 64-bit range.
+  const long long max_nodes = 4 * kScratchDoubles;
+  if (nx > max_nodes || ny > max_nodes || nz > max_nodes || (long long)nx * ny > max_nodes ||
+      (long long)nx * ny * nz > max_nodes) {
+    char msg[200];
+    std::snprintf(msg, sizeof msg,
+                  "e3d_apply_noalloc: a %dx%dx%d grid cannot fit in E3D_NOALLOC_SCRATCH_BYTES = %lld "
+                  "(at most %lld nodes)",
+                  nx, ny, nz, (long long)E3D_NOALLOC_SCRATCH_BYTES, max_nodes);
+    e3d_record_error_text(msg);
+    return E3D_ERR_INPUT;
+  }
+  {
+    // y = K x is formed in place of y while other blocks still read x
+    const uintptr_t xb = reinterpret_cast<uintptr_t>(d_x), yb = reinterpret_cast<uintptr_t>(d_y);
+    const uintptr_t bytes = (uintptr_t)(3LL * nx * ny * nz) * sizeof(double);
+    if (xb < yb + bytes && yb < xb + bytes) {
+      e3d_record_error_text("e3d_apply_noalloc: d_x and d_y overlap; y = K x needs separate buffers");
+      return E3D_ERR_INPUT;
+    }
+  }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail("cudaGetDevice", e);
-  if (dev < 0 || dev >= kMaxDevices) return E3D_ERR_INPUT;
+  if (dev < 0 || dev >= kMaxDevices) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "e3d_apply_noalloc: device %d is beyond the %d devices this entry point serves",
+                  dev, kMaxDevices);
+    e3d_record_error_text(msg);
+    return E3D_ERR_INPUT;
+  }
   int num_sms = 0;
   if ((e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
     return fail("cudaDeviceGetAttribute", e);

@@ -216,14 +216,17 @@ int32_t e3d_stencil_path(const e3d_handle_t* h);
  *   d_pix  ns int32 phase ids, 1-based, in [1, nphase] (checked),
  *   d_cmod 36*nphase doubles, cmod(nphase,6,6) in the reference layout
  *          (e3d_get_cmod returns it),
- *   d_x, d_y 3*ns doubles (SoA),
+ *   d_x, d_y 3*ns doubles (SoA), in separate buffers (overlapping ones are
+ *          refused with E3D_ERR_INPUT: y is written while x is still read),
  * and the scaled stiffness table and tile halos live in one static device
  * array of E3D_NOALLOC_SCRATCH_BYTES per GPU, held from library load to
  * process exit.  A grid whose scratch (about 41*3*ns/256 doubles of halos plus
  * 108*(nphase+1) doubles of table -- e.g. 128^3 with up to 4096 phases) does
  * not fit is rejected with E3D_ERR_INPUT and e3d_last_cuda_error() says why.
  * Runs on `stream` (a cudaStream_t, NULL = legacy default) of the current
- * device and returns after it completes.  The first call on each device looks
+ * device; each call copies a phase-check flag back to host memory and waits
+ * for `stream` before it returns, so y is complete on return.  Every
+ * rejection leaves its reason in e3d_last_cuda_error().  The first call on each device looks
  * up the array's device address (make it before any stream capture).  Calls
  * share the array: calls that overlap on the GPU race. */
 #define E3D_NOALLOC_SCRATCH_BYTES (16LL * 1024 * 1024)

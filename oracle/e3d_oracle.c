@@ -24,7 +24,12 @@
 #include <omp.h>
 #endif
 
-#define RCHUNK 4096 /* deterministic reduction chunk */
+/* Deterministic reductions: fixed-size chunk partials summed in order.  The
+ * chunk length only changes the rounding of the sums; tests set another one
+ * to see how far two equally valid FP64 summation orders drift apart along a
+ * solve. */
+static size_t RCHUNK = 4096;
+void orc_set_reduction_chunk(int64_t n) { RCHUNK = n > 0 ? (size_t)n : 4096; }
 
 static double wtime(void) {
 #ifdef _OPENMP
@@ -608,71 +613,125 @@ static void precond(const double* minv, const double* g, double* z, size_t ns) {
                       minv[m + ns * (i + 6)] * g[m + 2 * ns];
 }
 
-int32_t orc_dembx(const orc_problem* p, const int32_t* pix, const int32_t* ib,
-                  const double* dk, double* u, double* gb, double* h, int32_t kkk,
-                  double gg0, int32_t max_steps, int32_t* lstep, double* gg_out,
-                  double* history, int32_t* reset_count) {
+/* State of one PCG solve (dembx_OpenMP, src/elas3dxtal_pcg.f90:1356-2043),
+ * split into set-up, iterations and tear-down so that a caller can time the
+ * iterations alone and run them in several calls without restarting the
+ * search direction.  u, gb and h stay caller-owned. */
+struct orc_pcg {
+  const orc_problem* p;
+  const int32_t *pix, *ib;
+  const double* dk;
+  double *u, *gb, *h, *Ah, *z, *minv, *history;
+  double gg, gg0_eff, rel_res_prev;
+  int32_t L, resets, reason, done;
+};
+
+orc_pcg* orc_pcg_begin(const orc_problem* p, const int32_t* pix, const int32_t* ib,
+                       const double* dk, double* u, double* gb, double* h, int32_t kkk,
+                       double gg0, double* history) {
   const size_t ns = (size_t)p->nx * p->ny * p->nz, n3 = 3 * ns;
-  double* Ah = (double*)malloc(sizeof(double) * n3);
-  double* z = (double*)malloc(sizeof(double) * n3);
-  double* minv = (double*)malloc(sizeof(double) * 9 * ns);
+  orc_pcg* s = (orc_pcg*)calloc(1, sizeof(orc_pcg));
+  if (!s) return NULL;
+  s->p = p, s->pix = pix, s->ib = ib, s->dk = dk, s->u = u, s->gb = gb, s->h = h, s->history = history;
+  s->Ah = (double*)malloc(sizeof(double) * n3);
+  s->z = (double*)malloc(sizeof(double) * n3);
+  s->minv = (double*)malloc(sizeof(double) * 9 * ns);
+  if (!s->Ah || !s->z || !s->minv) {
+    orc_pcg_end(s, NULL, NULL, NULL);
+    return NULL;
+  }
   /* kkk == 1 builds the preconditioner (src/elas3dxtal_pcg.f90:1498-1520);
    * kmax = 1 in the reference so it is always built here.  precond == 1 is the
    * unpreconditioned CG of applications/sec3_1/cg/n_100x100x100/elas3dxtal_cg.f90:
    * 1011-1060 (z = g, no divergence reset). */
   if (p->precond == 1) {
-    memset(minv, 0, sizeof(double) * 9 * ns);
-    for (size_t m = 0; m < ns; ++m) minv[m] = minv[m + 4 * ns] = minv[m + 8 * ns] = 1.0;
+    memset(s->minv, 0, sizeof(double) * 9 * ns);
+    for (size_t m = 0; m < ns; ++m) s->minv[m] = s->minv[m + 4 * ns] = s->minv[m + 8 * ns] = 1.0;
   } else {
-    orc_block_jacobi(p, pix, ib, dk, minv);
+    orc_block_jacobi(p, pix, ib, dk, s->minv);
   }
-  precond(minv, gb, z, ns);
-  double gg = ddot(z, gb, n3);
-  if (kkk == 1) memcpy(h, z, sizeof(double) * n3);
-  const double gg0_eff = (p->criterion == 1) ? gg : gg0;
-  double rel_res_prev = sqrt(gg / gg0_eff);
-  int32_t resets = 0, L = 0, reason = 2;
+  precond(s->minv, gb, s->z, ns);
+  s->gg = ddot(s->z, gb, n3);
+  if (kkk == 1) memcpy(h, s->z, sizeof(double) * n3);
+  s->gg0_eff = (p->criterion == 1) ? s->gg : gg0;
+  s->rel_res_prev = sqrt(s->gg / s->gg0_eff);
+  s->reason = 2;
+  return s;
+}
+
+int32_t orc_pcg_iterate(orc_pcg* s, int32_t nsteps) {
+  const orc_problem* p = s->p;
+  const size_t ns = (size_t)p->nx * p->ny * p->nz, n3 = 3 * ns;
+  double *u = s->u, *gb = s->gb, *h = s->h, *Ah = s->Ah, *z = s->z;
   const double tol = (double)p->tol;
-  const int32_t limit = (max_steps > 0 && max_steps < p->ldemb) ? max_steps : p->ldemb;
-  for (int32_t ijk = 1; ijk <= limit; ++ijk) {
-    L++;
-    orc_apply(p, pix, ib, dk, h, Ah);
-    const double hAh = ddot(h, Ah, n3);
-    if (fabs(hAh) < 1e-14) {
-      reason = 1;
+  for (int32_t k = 0; k < nsteps && !s->done; ++k) {
+    if (s->L >= p->ldemb) { /* ldemb iterations done (:1574) */
+      s->reason = 2;
+      s->done = 1;
       break;
     }
-    const double lambda = gg / hAh;
+    s->L++;
+    orc_apply(p, s->pix, s->ib, s->dk, h, Ah);
+    const double hAh = ddot(h, Ah, n3);
+    if (fabs(hAh) < 1e-14) {
+      s->reason = 1;
+      s->done = 1;
+      break;
+    }
+    const double lambda = s->gg / hAh;
 #pragma omp parallel for schedule(guided)
     for (size_t i = 0; i < n3; ++i) {
       u[i] = u[i] - lambda * h[i];
       gb[i] = gb[i] - lambda * Ah[i];
     }
-    precond(minv, gb, z, ns);
-    const double gglast = gg;
-    gg = ddot(z, gb, n3);
-    const double rel_res = sqrt(gg / gg0_eff);
-    if (history) history[L - 1] = rel_res;
-    if (p->divergence_reset && rel_res > 10.0 * rel_res_prev && L > 1) {
+    precond(s->minv, gb, z, ns);
+    const double gglast = s->gg;
+    s->gg = ddot(z, gb, n3);
+    const double rel_res = sqrt(s->gg / s->gg0_eff);
+    if (s->history) s->history[s->L - 1] = rel_res;
+    if (p->divergence_reset && rel_res > 10.0 * s->rel_res_prev && s->L > 1) {
       memcpy(h, z, sizeof(double) * n3);
-      resets++;
+      s->resets++;
     } else {
-      const double gamma = gg / gglast;
+      const double gamma = s->gg / gglast;
 #pragma omp parallel for schedule(guided)
       for (size_t i = 0; i < n3; ++i) h[i] = z[i] + gamma * h[i];
     }
-    rel_res_prev = rel_res;
+    s->rel_res_prev = rel_res;
     if (rel_res < tol) {
-      reason = 0;
+      s->reason = 0;
+      s->done = 1;
       break;
     }
   }
-  *lstep = L;
-  *gg_out = gg;
-  if (reset_count) *reset_count = resets;
-  free(Ah);
-  free(z);
-  free(minv);
+  if (!s->done && s->L >= p->ldemb) {
+    s->reason = 2;
+    s->done = 1;
+  }
+  return s->done ? s->reason : -1;
+}
+
+void orc_pcg_end(orc_pcg* s, int32_t* lstep, double* gg_out, int32_t* reset_count) {
+  if (!s) return;
+  if (lstep) *lstep = s->L;
+  if (gg_out) *gg_out = s->gg;
+  if (reset_count) *reset_count = s->resets;
+  free(s->Ah);
+  free(s->z);
+  free(s->minv);
+  free(s);
+}
+
+int32_t orc_dembx(const orc_problem* p, const int32_t* pix, const int32_t* ib,
+                  const double* dk, double* u, double* gb, double* h, int32_t kkk,
+                  double gg0, int32_t max_steps, int32_t* lstep, double* gg_out,
+                  double* history, int32_t* reset_count) {
+  orc_pcg* s = orc_pcg_begin(p, pix, ib, dk, u, gb, h, kkk, gg0, history);
+  if (!s) return -1;
+  const int32_t limit = (max_steps > 0 && max_steps < p->ldemb) ? max_steps : p->ldemb;
+  int32_t reason = orc_pcg_iterate(s, limit);
+  if (reason < 0) reason = 2;
+  orc_pcg_end(s, lstep, gg_out, reset_count);
   return reason;
 }
 

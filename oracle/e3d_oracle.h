@@ -95,6 +95,17 @@ int32_t orc_dembx(const orc_problem* p, const int32_t* pix, const int32_t* ib,
                   int32_t kkk, double gg0, int32_t max_steps, int32_t* lstep,
                   double* gg_out, double* history, int32_t* reset_count);
 
+/* The same solve in three steps: set-up (block-Jacobi build, z0, gg,
+ * h = z0), nsteps iterations per orc_pcg_iterate call (the search direction
+ * carries over between calls), and tear-down.  orc_pcg_iterate returns the
+ * exit reason once the solve has ended and -1 while it is still running. */
+typedef struct orc_pcg orc_pcg;
+orc_pcg* orc_pcg_begin(const orc_problem* p, const int32_t* pix, const int32_t* ib,
+                       const double* dk, double* u, double* gb, double* h,
+                       int32_t kkk, double gg0, double* history);
+int32_t orc_pcg_iterate(orc_pcg* s, int32_t nsteps);
+void orc_pcg_end(orc_pcg* s, int32_t* lstep, double* gg_out, int32_t* reset_count);
+
 /* Volume-averaged stress and engineering strain, Voigt xx,yy,zz,xz,yz,xy
  * (stress_OpenMP, :2149-2408). */
 void orc_stress(const orc_problem* p, const int32_t* pix, const double* cmod,
@@ -123,6 +134,11 @@ int32_t orc_run(const orc_problem* p, const int32_t* pix, const double* rod,
                 double* u, double* history, orc_result* res);
 
 int32_t orc_num_threads(void);
+
+/* Length of the chunks whose partial sums make every dot product (default
+ * 4096; n <= 0 restores it).  Another length gives another, equally valid,
+ * FP64 summation order. */
+void orc_set_reduction_chunk(int64_t n);
 
 #ifdef __cplusplus
 }

@@ -80,12 +80,20 @@ def lib():
         L.orc_dembx.argtypes = [pp, ip, ip, dp, dp, dp, dp, C.c_int32, C.c_double, C.c_int32,
                                 ip, dp, dp, ip]
         L.orc_dembx.restype = C.c_int32
+        L.orc_pcg_begin.argtypes = [pp, ip, ip, dp, dp, dp, dp, C.c_int32, C.c_double, dp]
+        L.orc_pcg_begin.restype = C.c_void_p
+        L.orc_pcg_iterate.argtypes = [C.c_void_p, C.c_int32]
+        L.orc_pcg_iterate.restype = C.c_int32
+        L.orc_pcg_end.argtypes = [C.c_void_p, ip, dp, ip]
+        L.orc_pcg_end.restype = None
         L.orc_stress.argtypes = [pp, ip, dp, dp, dp, dp]
         L.orc_stress_fullfield.argtypes = [pp, ip, dp, dp, dp, dp]
         L.orc_assig.argtypes = [pp, ip, dp]
         L.orc_run.argtypes = [pp, ip, dp, dp, dp, C.POINTER(OrcResult)]
         L.orc_run.restype = C.c_int32
         L.orc_num_threads.restype = C.c_int32
+        L.orc_set_reduction_chunk.argtypes = [C.c_int64]
+        L.orc_set_reduction_chunk.restype = None
         _lib = L
     return _lib
 
@@ -211,6 +219,10 @@ class Oracle:
         return dict(u=u, g=g, lstep=L.value, gg=gg.value, history=hist[: L.value].copy(),
                     reason=reason, resets=resets.value)
 
+    def pcg(self, u, g, gg0):
+        """A PCG solve that runs in steps (see PCG)."""
+        return PCG(self, u, g, gg0)
+
     def stress(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
         s = np.zeros(6)
@@ -230,6 +242,41 @@ class Oracle:
         prob = np.zeros(self.p.nphase)
         lib().orc_assig(C.byref(self.cp), _ip(self.pix), _dp(prob))
         return prob
+
+
+class PCG:
+    """dembx_OpenMP (src/elas3dxtal_pcg.f90:1356-2043) in steps: the constructor
+    builds the block-Jacobi inverse, z0 = Minv g0 and h = z0; iterate(n) runs n
+    more iterations with the search direction carried over; close() frees the
+    work arrays.  u and g are copied in and updated in place (``.u``, ``.g``)."""
+
+    def __init__(self, o: "Oracle", u, g, gg0: float):
+        self._o = o
+        self.u = np.ascontiguousarray(u, dtype=np.float64).copy()
+        self.g = np.ascontiguousarray(g, dtype=np.float64).copy()
+        self.h = np.zeros_like(self.u)
+        self.history = np.zeros(max(o.p.ldemb, 1))
+        self._s = lib().orc_pcg_begin(C.byref(o.cp), _ip(o.pix), _ip(o.ib), _dp(o.dk), _dp(self.u),
+                                      _dp(self.g), _dp(self.h), 1, float(gg0), _dp(self.history))
+        if not self._s:
+            raise MemoryError("oracle PCG set-up failed (allocation)")
+        self.reason = -1
+
+    def iterate(self, n: int) -> int:
+        """Runs up to n iterations; returns the exit reason once the solve has
+        ended (0 converged, 1 hAh guard, 2 ldemb), else -1."""
+        self.reason = lib().orc_pcg_iterate(self._s, int(n))
+        return self.reason
+
+    def close(self) -> dict:
+        L = C.c_int32(0)
+        gg = C.c_double(0.0)
+        resets = C.c_int32(0)
+        if self._s:
+            lib().orc_pcg_end(self._s, C.byref(L), C.byref(gg), C.byref(resets))
+            self._s = None
+        return dict(lstep=L.value, gg=gg.value, resets=resets.value, reason=self.reason,
+                    history=self.history[: L.value].copy())
 
 
 def run(prob: Problem, pix: np.ndarray, rod: np.ndarray):
@@ -271,3 +318,8 @@ def invert3x3(a: np.ndarray) -> np.ndarray:
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+def set_reduction_chunk(n: int) -> None:
+    """Chunk length of the oracle's dot products (0 restores the default 4096)."""
+    lib().orc_set_reduction_chunk(int(n))

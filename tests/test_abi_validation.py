@@ -70,3 +70,25 @@ def test_batch_and_server_reject_bad_arguments(L):
     so.round_iters = 0
     assert B.e3d_serve_create(C.byref(h), C.byref(so)) == e3d.E3D_ERR_INPUT
     assert B.e3d_serve_submit(None, C.byref(good), e3d._dp(np.zeros(6)), None) == e3d.E3D_ERR_INPUT
+
+
+def test_apply_noalloc_rejects_before_any_cuda_call(L):
+    """The allocation-free K.x refuses malformed calls before it touches the
+    device (the pointers below are never dereferenced) and says why."""
+    fake = [C.c_void_p(0x10000000 + 0x100000 * k) for k in range(4)]  # pix, cmod, x, y
+    big = 2 ** 31 - 1
+    # sizes whose tile arithmetic would overflow a 32-bit int
+    for dims in [(big, 1, 1), (1, big, 1), (1, 1, big), (big, big, big), (65536, 65536, 2)]:
+        assert L.e3d_apply_noalloc(*dims, 3, *fake, None) == e3d.E3D_ERR_INPUT
+        assert "E3D_NOALLOC_SCRATCH_BYTES" in e3d.last_cuda_error()
+    assert L.e3d_apply_noalloc(0, 4, 4, 3, *fake, None) == e3d.E3D_ERR_INPUT
+    assert "at least 1" in e3d.last_cuda_error()
+    assert L.e3d_apply_noalloc(4, 4, 4, 3, None, *fake[1:], None) == e3d.E3D_ERR_INPUT
+    assert "NULL" in e3d.last_cuda_error()
+    # y = K x cannot be formed in place: x and y must not overlap
+    ns = 8 * 8 * 8
+    x = 0x20000000
+    for y in (x, x + 8 * (3 * ns - 1), x - 8 * (3 * ns - 1)):
+        rc = L.e3d_apply_noalloc(8, 8, 8, 3, fake[0], fake[1], C.c_void_p(x), C.c_void_p(y), None)
+        assert rc == e3d.E3D_ERR_INPUT
+        assert "overlap" in e3d.last_cuda_error()

@@ -147,6 +147,8 @@ def test_full_solve_polycrystal(criterion):
     assert _rel(res["epsav"], ref["epsav"]) < SOLVE_TOL
     hist = g.history()
     assert hist.size == res["iterations"]
+    n = min(hist.size, ref["history"].size)
+    assert np.max(np.abs(hist[:n] - ref["history"][:n]) / ref["history"][:n]) < 1e-6
     g.close()
 
 

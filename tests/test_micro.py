@@ -153,3 +153,22 @@ def test_driver_help_runs_without_gpu():
     drv = os.path.join(os.path.dirname(e3d.LIB_PATH), "e3d_run")
     out = subprocess.run([drv, "--help"], capture_output=True, text=True)
     assert out.returncode == 0 and "--generate" in out.stdout
+
+
+def test_oracle_side_workload_equals_package_workload():
+    """The CPU arms of the bench build their input with the generator compiled
+    on its own (oracle/workload.py, no CUDA library); it must be bit for bit the
+    input the package builds."""
+    import oracle as O
+    import workload as OW
+    from elas3d_xtal_gb300 import workloads as W
+
+    for n in (24, 41):
+        p, pix, rod = W.c2(n=n)
+        op, opix, orod = OW.c2(n=n)
+        assert np.array_equal(pix, opix) and np.array_equal(rod, orod)
+        assert (op.nx, op.ny, op.nz, op.nphase) == (p.nx, p.ny, p.nz, p.nphase)
+        assert (op.c11, op.c12, op.c44, op.flag_m) == (p.c11, p.c12, p.c44, p.flag_m)
+        assert (op.exx, op.eyy, op.ezz, op.exz, op.eyz, op.exy) == tuple(p.strain)
+        assert np.float32(op.tol) == np.float32(p.tol)
+        assert isinstance(op, O.Problem)

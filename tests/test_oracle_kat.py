@@ -237,3 +237,39 @@ def test_divergence_reset_and_criterion_variants_run():
             p.criterion, p.divergence_reset = crit, reset
             r = O.run(p, pix, rod)
             assert r["exit_reason"] == 0 and r["lstep"] > 0
+
+
+def test_reduction_order_changes_rounding_only():
+    """Another chunk length for the oracle's dot products is another valid FP64
+    summation order: the solve ends at the same energy to rounding, the
+    history agrees closely, and the default comes back with 0."""
+    p, pix, rod, _ = _rand_problem(10, 9, 8, 5, seed=41, strain=[1e-3, 0, 0, 0, 2e-4, 0])
+    a = O.run(p, pix, rod)
+    try:
+        O.set_reduction_chunk(64)
+        b = O.run(p, pix, rod)
+    finally:
+        O.set_reduction_chunk(0)
+    c = O.run(p, pix, rod)
+    assert abs(a["utot"] - b["utot"]) <= 1e-12 * abs(a["utot"])
+    assert abs(a["lstep"] - b["lstep"]) <= 1
+    n = min(a["history"].size, b["history"].size)
+    assert np.max(np.abs(a["history"][:n] - b["history"][:n]) / a["history"][:n]) < 1e-6
+    assert np.array_equal(a["history"], c["history"]) and a["utot"] == c["utot"]
+
+
+def test_pcg_in_steps_equals_dembx():
+    """The stepwise PCG (set-up, iterations in several calls, tear-down) is the
+    same solve as one dembx call, bit for bit."""
+    p, pix, rod, _ = _rand_problem(7, 6, 5, 3, seed=43, strain=[0, 5e-4, 0, 0, 0, 1e-4])
+    o = O.Oracle(p, pix, rod).femat()
+    u = o.affine_u()
+    g, _ = o.energy(u)
+    gg0 = float(g @ g)
+    r = o.dembx(u, g, gg0)
+    s = o.pcg(u, g, gg0)
+    while s.iterate(3) < 0:
+        pass
+    d = s.close()
+    assert d["lstep"] == r["lstep"] and d["reason"] == r["reason"] == 0
+    assert np.array_equal(s.u, r["u"]) and np.array_equal(d["history"], r["history"])
