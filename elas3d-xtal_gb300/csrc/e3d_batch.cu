@@ -253,7 +253,8 @@ struct Engine {
   int32_t init(int device) {
     int per_sm = 0, sms = 0;
     BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, job_engine_kernel, NT, 0));
+    BCUDA(cudaFuncSetAttribute(job_engine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kEngineDynSmem));
+    BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, job_engine_kernel, NT, kEngineDynSmem));
     if (per_sm < 1) return E3D_ERR_CUDA;
     grid = per_sm * sms;
     BCUDA(cudaMalloc(&d_head, 256));
@@ -316,7 +317,7 @@ struct Engine {
     E.err = d_err;
     E.it_limit = it_limit;
     E.timeout_ns = kTimeoutNs;
-    job_engine_kernel<<<grid, NT, 0, s>>>(E);
+    job_engine_kernel<<<grid, NT, kEngineDynSmem, s>>>(E);
     BCUDA(cudaGetLastError());
     return E3D_OK;
   }

@@ -341,14 +341,20 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
   const long long ns = h->G.ns, n3 = 3 * ns;
   const int np = p->nphase;
   // PCG grid: as many co-resident tile blocks as the device holds.
+  // (phase B of the per-thread-load kernels streams through dynamic shared memory)
   int per_sm = 0;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel<double>, NT, 0)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(pcg_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                pcg_dyn_smem_bytes<double>())) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_persistent_kernel<double>, NT,
+                                                         pcg_dyn_smem_bytes<double>())) != cudaSuccess)
     return fail(cuda_fail(e, "occupancy"));
   if (per_sm < 1) return fail(E3D_ERR_CUDA);
   h->pcg_grid = per_sm * h->num_sms;
   int per_sm32 = 0;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, pcg_persistent_kernel<float>, NT, 0)) !=
-      cudaSuccess)
+  if ((e = cudaFuncSetAttribute(pcg_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                pcg_dyn_smem_bytes<float>())) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, pcg_persistent_kernel<float>, NT,
+                                                         pcg_dyn_smem_bytes<float>())) != cudaSuccess)
     return fail(cuda_fail(e, "occupancy"));
   if (per_sm32 < 1) return fail(E3D_ERR_CUDA);
   h->pcg_grid32 = per_sm32 * h->num_sms;
@@ -687,7 +693,8 @@ int32_t launch_pcg(e3d_handle* h, int it_limit) {
   E3D_CUDA(cudaMemsetAsync(h->bar, 0, sizeof(GridBarrier), h->stream));
   void* args[] = {&P};
   const void* fn = tma ? (const void*)pcg_persistent_kernel<float, true> : (const void*)pcg_persistent_kernel<T>;
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NT), args, tma ? kRingSmemBytes : 0, h->stream);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NT), args,
+                                              tma ? kRingSmemBytes : pcg_dyn_smem_bytes<T>(), h->stream);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(pcg)");
   return E3D_OK;

@@ -317,11 +317,24 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
   return hAh;
 }
 
+// Phase-B planes in flight per thread through cp.async stages in the engine's
+// dynamic shared memory (0: the one-node register form).
+#ifndef E3D_ENGINE_PB_ASYNC
+#define E3D_ENGINE_PB_ASYNC 2
+#endif
+constexpr int kEngineDynSmem = E3D_ENGINE_PB_ASYNC > 0 ? pb_async_bytes<float, E3D_ENGINE_PB_ASYNC, true>() : 0;
+
 // du -= lam h, g -= lam Ah, z = Minv g: returns this part's z.g.
-static __device__ __noinline__ double job_fp32_update(const JobDesc& J, int part, float lam, int cur) {
-  return pcg_update_tiles<float>(J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah,
-                                 reinterpret_cast<const float*>(J.hx), reinterpret_cast<const float*>(J.hy),
-                                 reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
+static __device__ __noinline__ double job_fp32_update(const JobDesc& J, int part, float lam, int cur, float* stages) {
+  if constexpr (E3D_ENGINE_PB_ASYNC > 0)
+    return pcg_update_tiles_async<float, E3D_ENGINE_PB_ASYNC, true>(
+        J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah, reinterpret_cast<const float*>(J.hx),
+        reinterpret_cast<const float*>(J.hy), reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32,
+        stages);
+  else
+    return pcg_update_tiles<float>(J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah,
+                                   reinterpret_cast<const float*>(J.hx), reinterpret_cast<const float*>(J.hy),
+                                   reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
 }
 
 static __device__ void job_fold(const JobDesc& J, int part) {
@@ -349,6 +362,8 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
   __shared__ int s_idx, s_part;
   __shared__ JobDesc sJ;
   __shared__ PcgState sS;
+  extern __shared__ __align__(128) unsigned char e3d_engine_dyn[];
+  float* pb_stages = reinterpret_cast<float*>(e3d_engine_dyn);  // kEngineDynSmem bytes
   ApplySmem<double>& sm64 = *reinterpret_cast<ApplySmem<double>*>(smraw);
   ApplySmem<float>& sm32 = *reinterpret_cast<ApplySmem<float>*>(smraw);
   const unsigned long long to = E.timeout_ns;
@@ -450,7 +465,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       __syncthreads();
       if (s.status != PCG_RUNNING) break;
       const float lam = (float)(s.gg / hAh);
-      const double zg = job_fp32_update(J, part, lam, cur);
+      const double zg = job_fp32_update(J, part, lam, cur, pb_stages);
       job_put(J, SL_B, part, zg, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double gg_new = job_reduce(J, SL_B, red);

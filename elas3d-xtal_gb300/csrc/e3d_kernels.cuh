@@ -61,6 +61,19 @@ constexpr int TILE_Y = 8;
 #ifndef E3D_F32_DEFER_U
 #define E3D_F32_DEFER_U 1
 #endif
+// Phase-B planes in flight per thread through cp.async stages (a power of two;
+// 0 keeps the one-node register form of pcg_update_tiles).
+#ifndef E3D_PB_ASYNC_F32
+#define E3D_PB_ASYNC_F32 4
+#endif
+#ifndef E3D_PB_ASYNC_F64
+#define E3D_PB_ASYNC_F64 2
+#endif
+// FP64 stencil: node sums share the adjoint butterflies between neighbouring
+// elements (9 instead of 11 additions per component and node).
+#ifndef E3D_F64_SHARED_ADJ
+#define E3D_F64_SHARED_ADJ 1
+#endif
 #ifndef E3D_PB_UNROLL_RING
 #define E3D_PB_UNROLL_RING (E3D_RING_ZS == 2 ? 4 : 1)  // phase-B nodes in flight per thread, ring kernel
 #endif
@@ -438,6 +451,9 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
 
   constexpr bool kPoldSmem = POLD_SMEM;
   constexpr bool kCarrySmem = sizeof(T) == 4 && E3D_F32_CARRY_SMEM != 0;
+  // FP64: the node sums share the adjoint's partial butterflies between
+  // neighbouring elements (see the node-sum step below).
+  constexpr bool kShareAdj = sizeof(T) == 8 && E3D_F64_SHARED_ADJ != 0;
   T Pold[3][4], carry[3][4];
   // FP32: the tile's share of h.Ah is summed in FP32 and added to the FP64
   // accumulator once per tile; FP64: every node's term goes straight into it.
@@ -508,7 +524,16 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
             carry[c][b] = hi;
           }
         }
-        if (k >= z0) had_xy_adj(lo, rr[c]);
+        if (k >= z0) {
+          if constexpr (kShareAdj) {  // rr = e0, e1, g0, g1 of had_xy_adj; the butterfly's last step is shared
+            rr[c][0] = lo[0] - lo[2];
+            rr[c][1] = lo[0] + lo[2];
+            rr[c][2] = lo[1] - lo[3];
+            rr[c][3] = lo[1] + lo[3];
+          } else {
+            had_xy_adj(lo, rr[c]);
+          }
+        }
         if constexpr (!kPoldSmem) {
 #pragma unroll
           for (int b = 0; b < 4; ++b) Pold[c][b] = Pn[c][b];
@@ -530,7 +555,71 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         hk[c][3] = (tx == wx - 1 && ty == wy - 1) ? cb[c * cst + o + TILE_X + 2] : T(0);
       }
     }
-    if (k >= z0) {
+    if (kShareAdj && k >= z0) {
+      // Node (x, y) collects r0(x,y) + r1(x-1,y) + r2(x,y-1) + r3(x-1,y-1) with
+      // r0 = e0 - g0, r1 = e0 + g0, r2 = e1 - g1, r3 = e1 + g1.  Grouped as
+      // E = e0(x,y) + e1(x,y-1), G = g0(x,y) + g1(x,y-1) (the element below
+      // hands over e1, g1 through shared memory) and then
+      // (E - G)(x,y) + (E + G)(x-1,y) (the lane to the left hands over E + G):
+      // 9 additions per component and node instead of 11.  Contributions from
+      // across the tile's low edges arrive through the halos, as before.
+      if (active) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          sm.r[2 * c + 0][tid] = rr[c][1];  // e1: to the element at y+1
+          sm.r[2 * c + 1][tid] = rr[c][3];  // g1
+        }
+      }
+      __syncthreads();
+      if (ty < wy) {  // warp-uniform: every lane of the row takes part in the shuffles
+        const int lz = k - z0;
+        T acc[3], pxv[3], hyv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          T E = T(0), Gs = T(0), e1 = T(0), g1 = T(0);
+          if (active) {
+            E = rr[c][0];
+            Gs = rr[c][2];
+            if (ty > 0) {
+              E += sm.r[2 * c + 0][tid - TILE_X];
+              Gs += sm.r[2 * c + 1][tid - TILE_X];
+            }
+            e1 = rr[c][1];
+            g1 = rr[c][3];
+          }
+          const T P = E + Gs;  // r1 + r3 of this column: to node (x+1, y)
+          const T R = e1 + g1;  // r3 alone: to node (x+1, y+1) of the next row
+          const T Pl = __shfl_up_sync(0xffffffffu, P, 1);
+          const T Rl = __shfl_up_sync(0xffffffffu, R, 1);
+          acc[c] = tx > 0 ? (E - Gs) + Pl : (E - Gs);
+          pxv[c] = P;
+          hyv[c] = tx > 0 ? (e1 - g1) + Rl : (e1 - g1);
+          rr[c][3] = R;
+        }
+        if (active) {
+          const long long m = E3D_IDX((long long)xg + (long long)G.nx * yg + nxy * wrapi(k, G.nz), ns);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) A.y[m + c * ns] = acc[c];
+          add_dot(hk[0][0] * acc[0] + hk[1][0] * acc[1] + hk[2][0] * acc[2]);
+          const long long hb = tile * htiles_stride + lz;
+          if (tx == wx - 1) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A.hx[E3D_IDX(((long long)c * G.ntiles * htiles_stride + hb) * TILE_Y + ty, halo_len(G, TILE_Y))] = pxv[c];
+            add_dot(hk[0][1] * pxv[0] + hk[1][1] * pxv[1] + hk[2][1] * pxv[2]);
+          }
+          if (ty == wy - 1) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A.hy[E3D_IDX(((long long)c * G.ntiles * htiles_stride + hb) * TILE_X + tx, halo_len(G, TILE_X))] = hyv[c];
+            add_dot(hk[0][2] * hyv[0] + hk[1][2] * hyv[1] + hk[2][2] * hyv[2]);
+          }
+          if (tx == wx - 1 && ty == wy - 1) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A.hd[E3D_IDX((long long)c * G.ntiles * htiles_stride + hb, halo_len(G, 1))] = rr[c][3];
+            add_dot(hk[0][3] * rr[0][3] + hk[1][3] * rr[1][3] + hk[2][3] * rr[2][3]);
+          }
+        }
+      }
+    } else if (k >= z0) {
       if (active) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -1434,6 +1523,177 @@ __device__ __forceinline__ double pcg_update_tiles(const GridDims& G, long long 
   return zg_t;
 }
 
+// ---------------------------------------------------------------------------
+// Phase B with its loads in flight through cp.async.  pcg_update_tiles keeps
+// one node's loads in registers at a time (the register cap set by the stencil
+// leaves nothing for more), so each thread waits a full memory latency per
+// node.  Here every thread streams its node column through S shared-memory
+// stages: the loads of plane lz + S - 1 are issued (cp.async, no registers held)
+// before plane lz is consumed, so S planes' worth of bytes stay in flight per
+// thread.  Each thread reads back only the slots it filled itself, so no block
+// barrier is needed: cp.async.wait_group orders a thread's own copies.  The
+// tile-edge halos (hx for lane 0 of each row, hy for row 0, hd for the corner
+// node) travel in the same stages.  Same additions in the same order as
+// pcg_update_tiles: the results are bitwise the same.
+__device__ __forceinline__ void cp_async_4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void cp_async_t(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 4)
+    cp_async_4(dst, src);
+  else
+    cp_async_8(dst, src);
+}
+
+// Values of one stage: per thread Ah 3, g 3, Minv 6 (and h 3, u 3 when u is
+// updated here), then the halo slots hx[3][TILE_Y], hy[3][TILE_X], hd[3].
+template <bool UPD_U>
+__host__ __device__ constexpr int pb_fields() {
+  return UPD_U ? 18 : 12;
+}
+template <bool UPD_U>
+__host__ __device__ constexpr int pb_stage_len() {
+  return pb_fields<UPD_U>() * NT + 3 * TILE_Y + 3 * TILE_X + 3;
+}
+template <typename T, int S, bool UPD_U>
+__host__ __device__ constexpr int pb_async_bytes() {
+  return S * pb_stage_len<UPD_U>() * (int)sizeof(T);
+}
+
+template <typename T, int S, bool UPD_U = true>
+__device__ __forceinline__ double pcg_update_tiles_async(const GridDims& G, long long first, long long stride, T lam,
+                                                         const T* __restrict__ hc, const T* __restrict__ Ah,
+                                                         const T* __restrict__ hx, const T* __restrict__ hy,
+                                                         const T* __restrict__ hd, const T* __restrict__ minv,
+                                                         T* __restrict__ u, T* __restrict__ g, T* __restrict__ z,
+                                                         T* __restrict__ stages) {
+  static_assert(S >= 2 && (S & (S - 1)) == 0, "stage count: a power of two");
+  constexpr int F = pb_fields<UPD_U>();
+  constexpr int SL = pb_stage_len<UPD_U>();
+  const long long ns = G.ns;
+  double zg_t = 0.0;
+  const int tid = threadIdx.x;
+  const int tx = tid % TILE_X, ty = tid / TILE_X;
+  const long long nxy = (long long)G.nx * G.ny;
+  const long long per_c = G.ntiles * G.tz;
+  for (long long t = first; t < G.ntiles; t += stride) {
+    const int tix = (int)(t % G.ntx);
+    const int tiy = (int)((t / G.ntx) % G.nty);
+    const int tiz = (int)(t / ((long long)G.ntx * G.nty));
+    const int x0 = tix * TILE_X, y0 = tiy * TILE_Y, z0 = tiz * G.tz;
+    const int wx = min(TILE_X, G.nx - x0), wy = min(TILE_Y, G.ny - y0), wz = min(G.tz, G.nz - z0);
+    if (tx >= wx || ty >= wy) continue;
+    const long long col = (long long)(x0 + tx) + (long long)G.nx * (y0 + ty);
+    // halo sources (the tiles at -x, -y and -x-y), as in halo_add_tile
+    const bool hxn = tx == 0, hyn = ty == 0;
+    const int txl = tix == 0 ? G.ntx - 1 : tix - 1;
+    const int tyd = tiy == 0 ? G.nty - 1 : tiy - 1;
+    const long long plane = (long long)tiz * G.nty;
+    const long long tX = (long long)txl + (long long)G.ntx * (tiy + plane);
+    const long long tY = (long long)tix + (long long)G.ntx * (tyd + plane);
+    const long long tD = (long long)txl + (long long)G.ntx * (tyd + plane);
+    auto issue = [&](int lz) {
+      T* d = stages + (lz & (S - 1)) * SL;
+      const long long m = E3D_IDX(col + nxy * (z0 + lz), ns);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cp_async_t<T>(d + c * NT + tid, Ah + m + c * ns);
+        cp_async_t<T>(d + (3 + c) * NT + tid, g + m + c * ns);
+      }
+#pragma unroll
+      for (int q = 0; q < 6; ++q) cp_async_t<T>(d + (6 + q) * NT + tid, minv + m + q * ns);
+      if constexpr (UPD_U) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          cp_async_t<T>(d + (12 + c) * NT + tid, hc + m + c * ns);
+          cp_async_t<T>(d + (15 + c) * NT + tid, u + m + c * ns);
+        }
+      }
+      T* hs = d + F * NT;
+      if (hxn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          cp_async_t<T>(hs + c * TILE_Y + ty, hx + E3D_IDX((c * per_c + tX * G.tz + lz) * TILE_Y + ty, 3 * per_c * TILE_Y));
+      }
+      if (hyn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          cp_async_t<T>(hs + 3 * TILE_Y + c * TILE_X + tx,
+                        hy + E3D_IDX((c * per_c + tY * G.tz + lz) * TILE_X + tx, 3 * per_c * TILE_X));
+      }
+      if (hxn && hyn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          cp_async_t<T>(hs + 3 * TILE_Y + 3 * TILE_X + c, hd + E3D_IDX(c * per_c + tD * G.tz + lz, 3 * per_c));
+      }
+    };
+#pragma unroll
+    for (int j = 0; j < S - 1; ++j) {
+      if (j < wz) issue(j);
+      cp_async_commit();
+    }
+    float zg32 = 0.f;  // FP32: this column's z.g, added to the FP64 sum once per tile
+    for (int lz = 0; lz < wz; ++lz) {
+      if (lz + S - 1 < wz) issue(lz + S - 1);
+      cp_async_commit();
+      cp_async_wait<S - 1>();  // plane lz has landed
+      const T* d = stages + (lz & (S - 1)) * SL;
+      const T* hs = d + F * NT;
+      T ah[3], gv[3], mi[6];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        ah[c] = d[c * NT + tid];
+        gv[c] = d[(3 + c) * NT + tid];
+      }
+#pragma unroll
+      for (int q = 0; q < 6; ++q) mi[q] = d[(6 + q) * NT + tid];
+      if (hxn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[c] += hs[c * TILE_Y + ty];
+      }
+      if (hyn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[c] += hs[3 * TILE_Y + c * TILE_X + tx];
+      }
+      if (hxn && hyn) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[c] += hs[3 * TILE_Y + 3 * TILE_X + c];
+      }
+      const long long m = E3D_IDX(col + nxy * (z0 + lz), ns);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if constexpr (UPD_U) u[m + c * ns] = d[(15 + c) * NT + tid] - lam * d[(12 + c) * NT + tid];
+        gv[c] = gv[c] - lam * ah[c];
+        g[m + c * ns] = gv[c];
+      }
+      const T z0v = mi[0] * gv[0] + mi[3] * gv[1] + mi[4] * gv[2];
+      const T z1v = mi[3] * gv[0] + mi[1] * gv[1] + mi[5] * gv[2];
+      const T z2v = mi[4] * gv[0] + mi[5] * gv[1] + mi[2] * gv[2];
+      z[m] = z0v;
+      z[m + ns] = z1v;
+      z[m + 2 * ns] = z2v;
+      if constexpr (sizeof(T) == 4)
+        zg32 += z0v * gv[0] + z1v * gv[1] + z2v * gv[2];
+      else
+        zg_t += (double)(z0v * gv[0] + z1v * gv[1] + z2v * gv[2]);
+    }
+    if constexpr (sizeof(T) == 4) zg_t += (double)zg32;
+  }
+  cp_async_wait<0>();
+  return zg_t;
+}
+
 // u -= lam h over the owned nodes of tiles first, first + stride, ... (the same
 // tile and column ownership as apply_tile and pcg_update_tiles).
 template <typename T>
@@ -1531,6 +1791,18 @@ static __device__ double reduce_broadcast(const double* partial, int n, double* 
   return s_val;
 }
 
+// Dynamic shared memory of the per-thread-load persistent kernel: the phase-B
+// cp.async stages (0 when phase B keeps its loads in registers).
+template <typename T>
+constexpr int pcg_dyn_smem_bytes() {
+  constexpr bool defer_u = sizeof(T) == 4 && E3D_F32_DEFER_U != 0;
+  constexpr int S = sizeof(T) == 4 ? E3D_PB_ASYNC_F32 : E3D_PB_ASYNC_F64;
+  if constexpr (S > 0)
+    return pb_async_bytes<T, S, !defer_u>();
+  else
+    return 0;
+}
+
 // T = double: the plain FP64 solve (u is the solution).  T = float: the inner
 // loop of the mixed-precision solve (u is the FP32 correction since the last
 // FP64 residual replacement; stencil, preconditioner and vectors in FP32, dot
@@ -1569,9 +1841,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
   __shared__ uint64_t ring_bars[E3D_TMA_STAGES];
   __shared__ RingCursor ring_cur;
   PlaneRing ring;
-  if constexpr (TMA) {
+  // per-thread-load form: phase B streams through cp.async stages in the
+  // dynamic shared memory (pcg_update_tiles_async)
+  constexpr int kPbStages = TMA ? 0 : (sizeof(T) == 4 ? E3D_PB_ASYNC_F32 : E3D_PB_ASYNC_F64);
+  T* pb_stages = nullptr;
+  {
     extern __shared__ __align__(128) unsigned char e3d_ring_smem[];
-    ring_setup(ring, e3d_ring_smem, ring_bars, &ring_cur, P.maps, P.err, P.timeout_ns);
+    if constexpr (TMA) ring_setup(ring, e3d_ring_smem, ring_bars, &ring_cur, P.maps, P.err, P.timeout_ns);
+    if constexpr (kPbStages > 0) pb_stages = reinterpret_cast<T*>(e3d_ring_smem);
   }
   // The PCG scalars live in shared memory: every thread reads them after a
   // barrier, thread 0 alone updates them (all blocks compute the same values
@@ -1637,8 +1914,13 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
     // (no index division); with kDeferU the u update waits for the next phase A.
     const T* hc = cur ? P.h0 : P.h1;  // the h_new of phase A
     constexpr int U = TMA ? E3D_PB_UNROLL_RING : (sizeof(T) == 4 ? E3D_PB_UNROLL_F32 : E3D_PB_UNROLL_F64);
-    const double zg_t = pcg_update_tiles<T, U, !kDeferU>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy,
-                                                         P.A.hd, P.minv, P.u, P.g, P.z);
+    double zg_t;
+    if constexpr (kPbStages > 0)
+      zg_t = pcg_update_tiles_async<T, kPbStages, !kDeferU>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy,
+                                                            P.A.hd, P.minv, P.u, P.g, P.z, pb_stages);
+    else
+      zg_t = pcg_update_tiles<T, U, !kDeferU>(G, blockIdx.x, gridDim.x, lam, hc, P.Ah, P.A.hx, P.A.hy, P.A.hd,
+                                              P.minv, P.u, P.g, P.z);
     if constexpr (kDeferU) {
       lam_pending = lam;
       h_pending = hc;
