@@ -59,6 +59,8 @@ EXPORTED_SYMBOLS = (
     "e3d_debug_bounds", "e3d_selftest_bounds", "e3d_strerror", "e3d_last_cuda_error",
     "e3d_apply_noalloc", "e3d_checkpoint_save", "e3d_checkpoint_load",
     "e3d_micro_write", "e3d_micro_read_header", "e3d_micro_read",
+    "e3d_h5_micro_info", "e3d_h5_micro_read", "e3d_h5_micro_write", "e3d_h5_fullfield_write",
+    "e3d_h5_dataset_size", "e3d_h5_read_i32", "e3d_h5_read_f64",
     "e3d_micro_grains", "e3d_micro_spherical_pores", "e3d_micro_ellipsoidal_pores",
     "e3d_micro_grains_device", "e3d_micro_spherical_pores_device", "e3d_micro_ellipsoidal_pores_device",
     "e3d_euler_to_rodrigues",
@@ -143,6 +145,17 @@ def load_library(path: str | None = None) -> C.CDLL:
     L.e3d_checkpoint_save.argtypes = [vp, C.c_char_p]
     L.e3d_checkpoint_load.argtypes = [vp, C.c_char_p]
     L.e3d_micro_write.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, dp]
+    i64p = C.POINTER(C.c_int64)
+    L.e3d_h5_micro_info.argtypes = [C.c_char_p, i64p, i64p, ip]
+    L.e3d_h5_micro_read.argtypes = [C.c_char_p, C.c_int64, C.c_int32, ip, dp]
+    L.e3d_h5_micro_write.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, dp]
+    L.e3d_h5_fullfield_write.argtypes = [C.c_char_p, C.c_int64, ip, dp, dp]
+    L.e3d_h5_dataset_size.argtypes = [C.c_char_p, C.c_char_p, i64p, ip, i64p]
+    L.e3d_h5_read_i32.argtypes = [C.c_char_p, C.c_char_p, C.c_int64, ip]
+    L.e3d_h5_read_f64.argtypes = [C.c_char_p, C.c_char_p, C.c_int64, dp]
+    for fn in (L.e3d_h5_micro_info, L.e3d_h5_micro_read, L.e3d_h5_micro_write, L.e3d_h5_fullfield_write,
+               L.e3d_h5_dataset_size, L.e3d_h5_read_i32, L.e3d_h5_read_f64):
+        fn.restype = C.c_int32
     L.e3d_micro_read_header.argtypes = [C.c_char_p, ip, ip, ip, ip]
     L.e3d_micro_read.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, dp]
     L.e3d_strerror.argtypes = [C.c_int32]
@@ -551,6 +564,72 @@ def micro_read(path):
     if rc != 0:
         raise ValueError(f"{path}: size or phase-range check failed ({rc})")
     return pix, rod, (nx, ny, nz)
+
+
+# HDF5 files (include/e3d_micro.h): the reference's input and full-field output
+def h5_micro_info(path):
+    """(npix, norient, (Nx, Ny, Nz) from the "dimensions" attribute or zeros)."""
+    L = load_library()
+    a, b = C.c_int64(), C.c_int64()
+    dims = np.zeros(3, np.int32)
+    rc = L.e3d_h5_micro_info(os.fsencode(path), C.byref(a), C.byref(b), _ip(dims))
+    if rc != 0:
+        raise OSError(f"{path}: {last_cuda_error()} ({rc})")
+    return a.value, b.value, tuple(int(v) for v in dims)
+
+
+def h5_micro_read(path, ns, ngrains):
+    """ppixel_hdf5: returns (pix, rod); raises on the reference's checks."""
+    L = load_library()
+    pix = np.empty(int(ns), np.int32)
+    rod = np.empty(max(3 * int(ngrains), 1))
+    rc = L.e3d_h5_micro_read(os.fsencode(path), int(ns), int(ngrains), _ip(pix), _dp(rod))
+    if rc != 0:
+        raise (OSError if rc == -1 else ValueError)(f"{path}: {last_cuda_error()} ({rc})")
+    return pix, rod[: 3 * int(ngrains)]
+
+
+def h5_micro_write(path, pix, rod, shape):
+    nx, ny, nz = shape
+    pix = np.ascontiguousarray(pix, dtype=np.int32).reshape(-1)
+    rod = np.ascontiguousarray(rod, dtype=np.float64).reshape(-1)
+    if pix.size != nx * ny * nz or rod.size % 3:
+        raise ValueError("pix must hold nx*ny*nz values and rod 3 per grain")
+    rc = load_library().e3d_h5_micro_write(os.fsencode(path), nx, ny, nz, rod.size // 3, _ip(pix),
+                                           _dp(rod) if rod.size else None)
+    if rc != 0:
+        raise OSError(f"{path}: {last_cuda_error()} ({rc})")
+
+
+def h5_fullfield_write(path, pix, vm, sigma):
+    pix = np.ascontiguousarray(pix, dtype=np.int32).reshape(-1)
+    vm = np.ascontiguousarray(vm, dtype=np.float64).reshape(-1)
+    sigma = np.ascontiguousarray(sigma, dtype=np.float64).reshape(-1)
+    if vm.size != pix.size or sigma.size != 6 * pix.size:
+        raise ValueError("vm must hold ns values and sigma 6*ns")
+    rc = load_library().e3d_h5_fullfield_write(os.fsencode(path), pix.size, _ip(pix), _dp(vm), _dp(sigma))
+    if rc != 0:
+        raise OSError(f"{path}: {last_cuda_error()} ({rc})")
+
+
+def h5_read(path, name):
+    """Dataset `name` of an HDF5 file as int32 or float64 (by its class),
+    shaped by its dimensions (HDF5 order)."""
+    L = load_library()
+    n, rank = C.c_int64(), C.c_int32()
+    dims = np.zeros(8, np.int64)
+    rc = L.e3d_h5_dataset_size(os.fsencode(path), name.encode(), C.byref(n), C.byref(rank),
+                               dims.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc != 0:
+        raise (OSError if rc == -1 else KeyError)(f"{path}: {last_cuda_error()} ({rc})")
+    shape = tuple(int(v) for v in dims[: rank.value])
+    out = np.empty(n.value, np.int32)
+    if L.e3d_h5_read_i32(os.fsencode(path), name.encode(), n.value, _ip(out)) != 0:
+        out = np.empty(n.value, np.float64)
+        rc = L.e3d_h5_read_f64(os.fsencode(path), name.encode(), n.value, _dp(out))
+        if rc != 0:
+            raise ValueError(f"{path}: {last_cuda_error()} ({rc})")
+    return out.reshape(shape)
 
 
 def euler_to_rodrigues(euler: np.ndarray) -> np.ndarray:

@@ -64,6 +64,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, 
     cu_units = ["e3d_gpu", "e3d_noalloc", "e3d_batch", "microgen_gpu"]
     cu_objs = [os.path.join(out, u + ".o") for u in cu_units]
     cpp_obj = os.path.join(out, "microgen.o")
+    h5_units = ["h5lite", "e3d_h5"]
+    h5_objs = [os.path.join(out, u + ".o") for u in h5_units]
     cu_cmds = []
     for u, o in zip(cu_units, cu_objs):
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *(["-DE3D_BOUNDS"] if bounds else []),
@@ -80,9 +82,12 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, 
             raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r.stdout + r.stderr
 
-    with ThreadPoolExecutor(len(cu_cmds) + 1) as ex:
-        logs = list(ex.map(run, [*cu_cmds, cpp_cmd]))
-    link = [nvcc, *ARCH, "-shared", "-o", lib + ".tmp", *cu_objs, cpp_obj, "-Xcompiler", "-fopenmp", "-lgomp"]
+    h5_cmds = [["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INCLUDE, "-c", os.path.join(CSRC, u + ".cpp"),
+                "-o", o] for u, o in zip(h5_units, h5_objs)]
+    with ThreadPoolExecutor(len(cu_cmds) + 1 + len(h5_cmds)) as ex:
+        logs = list(ex.map(run, [*cu_cmds, cpp_cmd, *h5_cmds]))
+    link = [nvcc, *ARCH, "-shared", "-o", lib + ".tmp", *cu_objs, cpp_obj, *h5_objs, "-Xcompiler", "-fopenmp",
+            "-lgomp"]
     logs.append(run(link))
     os.replace(lib + ".tmp", lib)
     if bounds:

@@ -5,9 +5,12 @@
 //   output_SS316L_polycrystal.txt   run log (:278-537)
 //   cg_history_polycrystal.txt      energy and rel_res per solve (:466-492)
 //   cgitr_SS316L_polycrystal.txt    rel_res per PCG iteration (:1458, :2019-2021)
-//   fullfield_poly.bin              pix, vm, stress_tensor(ns,6) -- the raw
-//                                   stand-in for fullfield_poly.h5 (:2840-2874)
+//   fullfield_poly.h5               pix, vm, stress_tensor(ns,6) (:2840-2874)
+// The microstructure comes from an HDF5 file with the datasets "pix" and
+// "orientation" (input_structure_poly.h5, read as ppixel_hdf5 reads it,
+// :2879-2990), from a .e3d container, or from the built-in generator.
 // Run `e3d_run --help` for the options.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -24,7 +27,9 @@ namespace {
 void usage() {
   std::printf(
       "usage: e3d_run [options]\n"
-      "  --input FILE.e3d          microstructure (pix + Rodrigues vectors)\n"
+      "  --input FILE              microstructure: HDF5 (\"pix\", \"orientation\"; grid from the\n"
+      "                            \"dimensions\" attribute or --grid) or .e3d\n"
+      "  --grid NX NY NZ           grid of an HDF5 input without a \"dimensions\" attribute\n"
       "  --generate N NGRAINS SEED PORE_FRAC   periodic Voronoi N^3 instead of --input\n"
       "  --c11 P --c12 P --c44 P   cubic constants in Pa (206e9 133e9 119e9)\n"
       "  --strain exx eyy ezz exz eyz exy      tensor macro strain (0 0 1e-3 0 0 0)\n"
@@ -35,7 +40,7 @@ void usage() {
       "  --isotropic E1 NU1        inclusion phase modulus / Poisson ratio (0 0)\n"
       "  --flag-m 0|1              0: isotropic matrix, 1: rotated cubic grains (1)\n"
       "  --outdir DIR              output directory (.)\n"
-      "  --fullfield               also write fullfield_poly.bin\n"
+      "  --fullfield               also write fullfield_poly.h5\n"
       "  --json                    print one JSON metrics line for the solve on stdout\n"
       "  --checkpoint FILE         save the PCG state at exit (resume with --resume)\n"
       "  --resume FILE             continue a saved solve\n"
@@ -53,7 +58,7 @@ int fail(const char* what, int rc) {
 
 int main(int argc, char** argv) {
   std::string input, outdir = ".", ckpt, resume;
-  int gen_n = 0, gen_g = 0;
+  int gen_n = 0, gen_g = 0, grid[3] = {0, 0, 0};
   unsigned long long gen_seed = 1;
   double gen_pores = 0.0;
   double c11 = 206.0e9, c12 = 133.0e9, c44 = 119.0e9, e1 = 0.0, nu1 = 0.0;
@@ -76,6 +81,13 @@ int main(int argc, char** argv) {
     } else if (a == "--input") {
       need(1);
       input = argv[++i];
+    } else if (a == "--grid") {
+      need(3);
+      for (int k = 0; k < 3; ++k) grid[k] = std::atoi(argv[++i]);
+      if (grid[0] < 1 || grid[1] < 1 || grid[2] < 1) {
+        usage();
+        return 2;
+      }
     } else if (a == "--generate") {
       need(4);
       gen_n = std::atoi(argv[++i]);
@@ -141,7 +153,45 @@ int main(int argc, char** argv) {
   int nx = 0, ny = 0, nz = 0, ng = 0;
   std::vector<int32_t> pix;
   std::vector<double> rod;
+  bool is_h5 = false;
   if (!input.empty()) {
+    if (FILE* f = std::fopen(input.c_str(), "rb")) {  // HDF5 format signature at 0 or after a user block
+      unsigned char sig[8];
+      for (long off = 0; !is_h5 && off <= 8192; off = off ? 2 * off : 512)
+        if (std::fseek(f, off, SEEK_SET) == 0 && std::fread(sig, 1, 8, f) == 8 &&
+            std::memcmp(sig, "\x89HDF\r\n\x1a\n", 8) == 0)
+          is_h5 = true;
+      std::fclose(f);
+    }
+  }
+  if (is_h5) {
+    int64_t npix = 0, nori = 0;
+    int32_t dims[3] = {0, 0, 0};
+    if (e3d_h5_micro_info(input.c_str(), &npix, &nori, dims) != 0) {
+      std::fprintf(stderr, "e3d_run: %s: %s\n", input.c_str(), e3d_last_cuda_error());
+      return 1;
+    }
+    if (grid[0] > 0) {
+      nx = grid[0], ny = grid[1], nz = grid[2];
+    } else if (dims[0] > 0 && dims[1] > 0 && dims[2] > 0) {
+      nx = dims[0], ny = dims[1], nz = dims[2];
+    } else {
+      std::fprintf(stderr, "e3d_run: %s has no \"dimensions\" attribute; give --grid NX NY NZ\n", input.c_str());
+      return 1;
+    }
+    if (nori % 3 != 0) {
+      std::fprintf(stderr, "e3d_run: %s: orientation holds %lld values, not 3 per grain\n", input.c_str(),
+                   (long long)nori);
+      return 1;
+    }
+    ng = (int)(nori / 3);
+    pix.resize((size_t)nx * ny * nz);
+    rod.resize(3 * (size_t)std::max(ng, 1));
+    if (e3d_h5_micro_read(input.c_str(), (int64_t)nx * ny * nz, ng, pix.data(), rod.data()) != 0) {
+      std::fprintf(stderr, "e3d_run: %s\n", e3d_last_cuda_error());
+      return 1;
+    }
+  } else if (!input.empty()) {
     if (e3d_micro_read_header(input.c_str(), &nx, &ny, &nz, &ng) != 0) {
       std::fprintf(stderr, "e3d_run: cannot read %s\n", input.c_str());
       return 1;
@@ -288,20 +338,14 @@ int main(int argc, char** argv) {
     std::fflush(stdout);
   }
   std::fclose(out);
-  if (fullfield) {  // stress_fullfield_OpenMP (:2639-2877) with a raw file instead of HDF5
+  if (fullfield) {  // stress_fullfield_OpenMP (:2639-2877)
     std::vector<double> sig(6 * (size_t)ns), vm((size_t)ns);
     if ((rc = e3d_stress_field(h, sig.data(), vm.data()))) return fail("e3d_stress_field", rc);
-    const std::string fp = outdir + "/fullfield_poly.bin";
-    FILE* f = std::fopen(fp.c_str(), "wb");
-    if (f) {
-      const char magic[8] = {'E', '3', 'D', 'F', 'I', 'E', 'L', 'D'};
-      const int32_t hdr[4] = {nx, ny, nz, 1};
-      std::fwrite(magic, 1, 8, f);
-      std::fwrite(hdr, sizeof(int32_t), 4, f);
-      std::fwrite(pix.data(), sizeof(int32_t), (size_t)ns, f);
-      std::fwrite(vm.data(), sizeof(double), (size_t)ns, f);
-      std::fwrite(sig.data(), sizeof(double), 6 * (size_t)ns, f);
-      std::fclose(f);
+    const std::string fp = outdir + "/fullfield_poly.h5";
+    if (e3d_h5_fullfield_write(fp.c_str(), (int64_t)ns, pix.data(), vm.data(), sig.data()) != 0) {
+      std::fprintf(stderr, "e3d_run: %s\n", e3d_last_cuda_error());
+      e3d_destroy(h);
+      return 1;
     }
   }
   e3d_destroy(h);

@@ -64,6 +64,50 @@ int32_t e3d_micro_read_header(const char* path, int32_t* nx, int32_t* ny,
 int32_t e3d_micro_read(const char* path, int32_t nx, int32_t ny, int32_t nz,
                        int32_t ngrains, int32_t* pix, double* rod);
 
+/* HDF5 files without libhdf5: a minimal reader and writer of the subset the
+ * HDF5 library writes by default (version-0/1 superblock, version-1 object
+ * headers, symbol-table root group, contiguous or compact datasets; chunked or
+ * filtered storage is refused).  Return 0 on success, -1 on I/O errors, -2 on
+ * a bad or unsupported file, -3 on a size mismatch, -4 on a phase id out of
+ * range; the reason is left in e3d_last_cuda_error (include/e3d_gpu.h).
+ *
+ * e3d_h5_micro_info: element counts of the datasets "pix" and "orientation"
+ * of a microstructure file and the int32 attribute "dimensions" of "pix"
+ * (Nx, Ny, Nz, as the reference's MATLAB generator stores it; zeros when
+ * absent).  dims may be NULL. */
+int32_t e3d_h5_micro_info(const char* path, int64_t* npix, int64_t* norient,
+                          int32_t dims[3]);
+
+/* ppixel_hdf5 (src/elas3dxtal_pcg.f90:2879-2990): reads "pix" (ns values,
+ * any integer type) and "orientation" (3*ngrains values, any float type) with
+ * the reference's checks -- the sizes must match (:2939-2942, :2966-2969)
+ * and every phase id must lie in [1, ngrains+1] (:2986-2989). */
+int32_t e3d_h5_micro_read(const char* path, int64_t ns, int32_t ngrains,
+                          int32_t* pix, double* rod);
+
+/* The input file of the reference's MATLAB generator
+ * (src/microstructure_gen.m:876-889): "pix" int32 (1 x ns, with the int32
+ * attribute "dimensions" = Nx, Ny, Nz) and "orientation" float64
+ * (1 x 3*ngrains, attribute "dimensions" = 3*ngrains, 1). */
+int32_t e3d_h5_micro_write(const char* path, int32_t nx, int32_t ny, int32_t nz,
+                           int32_t ngrains, const int32_t* pix, const double* rod);
+
+/* fullfield_poly.h5 of stress_fullfield_OpenMP (src/elas3dxtal_pcg.f90:
+ * 2840-2874): "pix" int32 (ns), "vm" float64 (ns) and "stress_tensor" float64
+ * (6 x ns in the file, i.e. the reference's stress_field(ns,6): component-major,
+ * the layout e3d_stress_field returns). */
+int32_t e3d_h5_fullfield_write(const char* path, int64_t ns, const int32_t* pix,
+                               const double* vm, const double* sigma);
+
+/* Any dataset of the root group by name: its element count, rank and
+ * dimensions (HDF5 order, slowest first; dims may be NULL, at most 8 filled),
+ * and its values converted to int32 / float64 (n must equal the count; -3 on a
+ * mismatch or an integer outside the int32 range). */
+int32_t e3d_h5_dataset_size(const char* path, const char* name, int64_t* count,
+                            int32_t* rank, int64_t dims[8]);
+int32_t e3d_h5_read_i32(const char* path, const char* name, int64_t n, int32_t* out);
+int32_t e3d_h5_read_f64(const char* path, const char* name, int64_t n, double* out);
+
 /* GPU versions of the three generators above: the same microstructures, bit
  * for bit, written to device memory.  d_pix: nx*ny*nz int32 on CUDA device
  * `device` (caller-owned; the pore routines read and update it in place);

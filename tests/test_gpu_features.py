@@ -77,16 +77,23 @@ def test_unpreconditioned_cg_variant_matches_oracle():
     assert abs(res["utot"] - ref["utot"]) <= 1e-9 * abs(ref["utot"])
 
 
-def test_driver_end_to_end(tmp_path):
+@pytest.mark.parametrize("fmt", ["h5", "e3d"])
+def test_driver_end_to_end(tmp_path, fmt):
+    """The driver reads the microstructure as ppixel_hdf5 does (an HDF5 file
+    with "pix" and "orientation", or the .e3d container) and writes the
+    reference's text outputs and fullfield_poly.h5."""
     drv = os.path.join(os.path.dirname(e3d.LIB_PATH), "e3d_run")
     pix, rod = e3d.micro_grains(14, 14, 14, 6, 4)
-    inp = str(tmp_path / "in.e3d")
-    e3d.micro_write(inp, pix, rod, (14, 14, 14))
+    inp = str(tmp_path / f"input_structure_poly.{fmt}")
+    if fmt == "h5":
+        e3d.h5_micro_write(inp, pix, rod, (14, 14, 14))
+    else:
+        e3d.micro_write(inp, pix, rod, (14, 14, 14))
     out = subprocess.run([drv, "--input", inp, "--outdir", str(tmp_path), "--fullfield", "--json",
                           "--strain", "1e-3", "0", "0", "0", "0", "0"], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
     for f in ("output_SS316L_polycrystal.txt", "cg_history_polycrystal.txt", "cgitr_SS316L_polycrystal.txt",
-              "fullfield_poly.bin"):
+              "fullfield_poly.h5"):
         assert os.path.getsize(tmp_path / f) > 0
     log = open(tmp_path / "output_SS316L_polycrystal.txt").read()
     op = O.Problem(14, 14, 14, 7, exx=1e-3, ezz=0.0)
@@ -100,5 +107,12 @@ def test_driver_end_to_end(tmp_path):
     assert metrics["utot"] == pytest.approx(ref["utot"], rel=1e-9)
     assert metrics["iterations"] == int(log.split("Number of conjugate steps=")[1].split()[0])
     assert metrics["dof"] == 3 * 14 ** 3 and metrics["precision"] == "fp64"
-    raw = np.fromfile(tmp_path / "fullfield_poly.bin", dtype=np.uint8)
-    assert raw.size == 8 + 16 + 4 * 14 ** 3 + 8 * 14 ** 3 * 7
+    ff = str(tmp_path / "fullfield_poly.h5")
+    assert np.array_equal(e3d.h5_read(ff, "pix"), pix)
+    o = O.Oracle(op, pix, rod).femat()
+    sig_ref, vm_ref = o.stress_fullfield(ref["u"])
+    sig = e3d.h5_read(ff, "stress_tensor")
+    assert sig.shape == (6, 14 ** 3)
+    den = np.linalg.norm(sig_ref)
+    assert np.linalg.norm(sig.ravel() - sig_ref) <= 1e-6 * den  # the converged fields of two solvers
+    assert np.linalg.norm(e3d.h5_read(ff, "vm") - vm_ref) <= 1e-6 * np.linalg.norm(vm_ref)
