@@ -40,7 +40,7 @@ struct JobDesc {
   // shared per RVE (read only)
   const int32_t* pix;  // global phase ids, 0-based into the batch tables
   const float* cs32;   // [phase][24] packed upper triangle of C/16
-  const double* cs64;  // [phase][108]
+  const double* cs64;  // [phase][kCsStride], modal_table
   const double* dk;    // [phase][576]
   const double* cmod;  // cmod(nphase_total,6,6), Fortran layout
   int nphase_total;
@@ -293,8 +293,11 @@ static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part
 #ifndef E3D_ENGINE_SWEEP_ATTR
 #define E3D_ENGINE_SWEEP_ATTR __noinline__
 #endif
+#ifndef E3D_ENGINE_TAB_ASYNC
+#define E3D_ENGINE_TAB_ASYNC 0  // stiffness rows staged one plane ahead (E3D_F32_TAB_ASYNC; slower there)
+#endif
 static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
-                                                     ApplySmem<float>& sm) {
+                                                     ApplySmem<float>& sm, float4* tab) {
   __shared__ ApplyArgs<float> sA;
   if (threadIdx.x == 0) {
     ApplyArgs<float> A = job_apply_args<float>(J);
@@ -311,7 +314,7 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
   const long long nt = J.G.ntiles;
   const int np = J.nparts;
   for (long long t = part; t < nt; t += np) {
-    apply_tile<float, true>(sA, t, sm, hAh);
+    apply_tile<float, true, E3D_F32_POLD_SMEM != 0, false, E3D_ENGINE_TAB_ASYNC != 0>(sA, t, sm, hAh, tab);
     __syncthreads();
   }
   return hAh;
@@ -322,7 +325,10 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
 #ifndef E3D_ENGINE_PB_ASYNC
 #define E3D_ENGINE_PB_ASYNC 2
 #endif
-constexpr int kEngineDynSmem = E3D_ENGINE_PB_ASYNC > 0 ? pb_async_bytes<float, E3D_ENGINE_PB_ASYNC, true>() : 0;
+constexpr int kEnginePbBytes =
+    E3D_ENGINE_PB_ASYNC > 0 ? pb_async_bytes<float, (E3D_ENGINE_PB_ASYNC > 0 ? E3D_ENGINE_PB_ASYNC : 2), true>() : 0;
+// the FP32 stencil's staged table rows share these bytes (the sweeps never overlap)
+constexpr int kEngineDynSmem = (E3D_ENGINE_TAB_ASYNC && kTabAsyncBytes > kEnginePbBytes) ? kTabAsyncBytes : kEnginePbBytes;
 
 // du -= lam h, g -= lam Ah, z = Minv g: returns this part's z.g.
 static __device__ __noinline__ double job_fp32_update(const JobDesc& J, int part, float lam, int cur, float* stages) {
@@ -449,7 +455,8 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
     const int it_end = min(s.it + E.it_limit, s.max_iter);
     while (ok && s.status == PCG_RUNNING && s.it < it_end) {
       const int cur = s.cur;
-      const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, sm32);
+      const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, sm32,
+                                          reinterpret_cast<float4*>(e3d_engine_dyn));
       job_put(J, SL_A, part, hAh_t, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double hAh = job_reduce(J, SL_A, red);
@@ -631,12 +638,8 @@ static __global__ void batch_phase_kernel(const PhaseMat* __restrict__ mats, int
       bond_rotate(M.r, M.c11, M.c12, M.c44, C6);
     }
     for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) {
-        cmod[p + (long long)nphase_total * (i + 6 * j)] = C6[i][j];
-        csh[6 * i + j] = C6[i][j] / 16.0;
-        csh[36 + 6 * i + j] = C6[i][j] / 48.0;
-        csh[72 + 6 * i + j] = C6[i][j] / 144.0;
-      }
+      for (int j = 0; j < 6; ++j) cmod[p + (long long)nphase_total * (i + 6 * j)] = C6[i][j];
+    modal_table(C6, csh);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) cs[(long long)p * kCsStride + i] = csh[i];

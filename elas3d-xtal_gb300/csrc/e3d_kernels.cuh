@@ -3,7 +3,7 @@
 //   u, g, b, z, h[2], Ah : 3*ns values each
 //   minv                 : 6*ns (symmetric 3x3 block inverse: 00 11 22 01 02 12)
 //   pix                  : ns int32, 0-based phase
-//   cs                   : nphase*108 scaled stiffness (C/16, C/48, C/144)
+//   cs                   : nphase*kCsStride FP64 stiffness tables (C/16 and the summed mode matrices)
 //   cs32                 : nphase*24, FP32 upper triangle of C/16 (element_modal_f32)
 //   dk                   : nphase*576, [p][a][i][b][j] (reference local order)
 //   dkd                  : nphase*72 diagonal 3x3 blocks [p][a][i][j]
@@ -69,6 +69,15 @@ constexpr int TILE_Y = 8;
 #ifndef E3D_PB_ASYNC_F64
 #define E3D_PB_ASYNC_F64 2
 #endif
+// FP32 stencil: each element's stiffness row staged in shared memory one plane
+// ahead through cp.async (per-thread-load persistent kernel).  Measured slower:
+// 500^3 inner iteration 8.41 ms against 5.68 ms with the rows read through the
+// read-only path, where a warp whose elements share a grain gets its row in
+// one broadcast access.
+#ifndef E3D_F32_TAB_ASYNC
+#define E3D_F32_TAB_ASYNC 0
+#endif
+constexpr int kTabAsyncBytes = 2 * 6 * 256 * 16;  // two slots of six float4 per thread (NT = 256)
 // FP64 stencil: node sums share the adjoint butterflies between neighbouring
 // elements (9 instead of 11 additions per component and node).
 #ifndef E3D_F64_SHARED_ADJ
@@ -342,8 +351,16 @@ __device__ __forceinline__ void ring_drain(PlaneRing& R) {
 // iteration (src/elas3dxtal_pcg.f90:1988-1995) folded into this pass -- and
 // h_new is stored for the tile's own nodes.  Returns this thread's share of
 // h_new . (K h_new) through hAh.
-template <typename T, bool FUSED, bool POLD_SMEM = (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), bool DEFER_U = false>
-__device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& sm, double& hAh) {
+//
+// TAB_ASYNC (FP32): each element's stiffness row is copied into a per-thread
+// shared-memory slot one plane ahead (cp.async, two slots alternating by plane
+// parity in `tab`, 2 x 6 x NT float4), so the gather's latency is off the
+// element's critical path.
+template <typename T, bool FUSED, bool POLD_SMEM = (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), bool DEFER_U = false,
+          bool TAB_ASYNC = false>
+__device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& sm, double& hAh,
+                           float4* __restrict__ tab = nullptr) {
+  static_assert(!TAB_ASYNC || sizeof(T) == 4, "the staged table rows are the FP32 ones");
   const GridDims& G = A.g;
   const int tid = threadIdx.x;
   const int tx = tid % TILE_X, ty = tid / TILE_X;
@@ -476,13 +493,43 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
   }
   prefetch(z0);
   int ph_cur = active ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(z0 - 1, G.nz), ns)) : 0;
+  // TAB_ASYNC: the row of element k sits in slot k & 1; ph_cur then holds the
+  // phase of element k + 1 (its row is copied during step k)
+  auto tab_issue = [&](int k, int ph) {
+    if constexpr (TAB_ASYNC) {
+      if (active) {
+        float4* d = tab + (k & 1) * 6 * NT + tid;
+        const float* src = reinterpret_cast<const float*>(A.cs) + E3D_IDX(ph, A.ncs) * kCs32Stride;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(
+                           (unsigned)__cvta_generic_to_shared(d + i * NT)),
+                       "l"(src + 4 * i)
+                       : "memory");
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+  };
+  if constexpr (TAB_ASYNC) {
+    tab_issue(z0 - 1, ph_cur);
+    ph_cur = (active && z0 < z0 + wz) ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(z0, G.nz), ns)) : 0;
+  }
   const int htiles_stride = G.tz;  // per-tile plane stride in halo buffers
   for (int k = z0 - 1; k < z0 + wz; ++k) {
     const bool own_next = (k + 1 >= z0) && (k + 1 < z0 + wz);
     commit(k + 1, own_next);
     __syncthreads();
     if (k + 2 <= z0 + wz) prefetch(k + 2);
-    const int ph_nxt = (active && k + 1 < z0 + wz) ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(k + 1, G.nz), ns)) : 0;
+    int ph_nxt;
+    if constexpr (TAB_ASYNC) {
+      // row of element k + 1 now, phase of element k + 2 for the next step
+      if (k + 1 < z0 + wz) tab_issue(k + 1, ph_cur);
+      else asm volatile("cp.async.commit_group;\n" ::: "memory");
+      ph_nxt = (active && k + 2 < z0 + wz) ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(k + 2, G.nz), ns)) : 0;
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // element k's row has landed
+    } else {
+      ph_nxt = (active && k + 1 < z0 + wz) ? __ldcs(A.pix + E3D_IDX(ecol + nxy * wrapi(k + 1, G.nz), ns)) : 0;
+    }
     T rr[3][4];
     if (active) {
       T nxt[3][4];
@@ -505,7 +552,10 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
         }
       }
       T f[3][8];
-      if constexpr (sizeof(T) == 4)
+      if constexpr (TAB_ASYNC)
+        element_modal_f32<NT>(reinterpret_cast<const float*>(tab + (k & 1) * 6 * NT + tid), h[0], h[1], h[2], f[0],
+                              f[1], f[2]);
+      else if constexpr (sizeof(T) == 4)
         element_modal_f32(A.cs + E3D_IDX(ph_cur, A.ncs) * kCs32Stride, h[0], h[1], h[2], f[0], f[1], f[2]);
       else
         element_modal<T>(A.cs + E3D_IDX(ph_cur, A.ncs) * kCsStride, h[0], h[1], h[2], f[0], f[1], f[2]);
@@ -667,6 +717,7 @@ __device__ void apply_tile(const ApplyArgs<T>& A, long long tile, ApplySmem<T>& 
     }
     ph_cur = ph_nxt;
   }
+  if constexpr (TAB_ASYNC) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   if constexpr (sizeof(T) == 4) hAh += (double)dot32;
 }
 
@@ -1125,12 +1176,8 @@ static __global__ void femat_phase_kernel(FematParams P, const double* __restric
       bond_rotate(r, P.c11, P.c12, P.c44, C6);
     }
     for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) {
-        cmod[p + (long long)P.nphase * (i + 6 * j)] = C6[i][j];
-        csh[6 * i + j] = C6[i][j] / 16.0;
-        csh[36 + 6 * i + j] = C6[i][j] / 48.0;
-        csh[72 + 6 * i + j] = C6[i][j] / 144.0;
-      }
+      for (int j = 0; j < 6; ++j) cmod[p + (long long)P.nphase * (i + 6 * j)] = C6[i][j];
+    modal_table(C6, csh);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < kCsStride; i += blockDim.x) cs[(long long)p * kCsStride + i] = csh[i];
@@ -1797,10 +1844,10 @@ template <typename T>
 constexpr int pcg_dyn_smem_bytes() {
   constexpr bool defer_u = sizeof(T) == 4 && E3D_F32_DEFER_U != 0;
   constexpr int S = sizeof(T) == 4 ? E3D_PB_ASYNC_F32 : E3D_PB_ASYNC_F64;
-  if constexpr (S > 0)
-    return pb_async_bytes<T, S, !defer_u>();
-  else
-    return 0;
+  constexpr int pb = S > 0 ? pb_async_bytes<T, (S > 0 ? S : 2), !defer_u>() : 0;
+  // phase A's staged table rows use the same bytes (the phases never overlap)
+  constexpr int tab = (sizeof(T) == 4 && E3D_F32_TAB_ASYNC != 0) ? kTabAsyncBytes : 0;
+  return pb > tab ? pb : tab;
 }
 
 // T = double: the plain FP64 solve (u is the solution).  T = float: the inner
@@ -1844,11 +1891,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
   // per-thread-load form: phase B streams through cp.async stages in the
   // dynamic shared memory (pcg_update_tiles_async)
   constexpr int kPbStages = TMA ? 0 : (sizeof(T) == 4 ? E3D_PB_ASYNC_F32 : E3D_PB_ASYNC_F64);
+  constexpr bool kTabAsync = sizeof(T) == 4 && !TMA && E3D_F32_TAB_ASYNC != 0;
   T* pb_stages = nullptr;
+  float4* tab_slots = nullptr;
   {
     extern __shared__ __align__(128) unsigned char e3d_ring_smem[];
     if constexpr (TMA) ring_setup(ring, e3d_ring_smem, ring_bars, &ring_cur, P.maps, P.err, P.timeout_ns);
     if constexpr (kPbStages > 0) pb_stages = reinterpret_cast<T*>(e3d_ring_smem);
+    if constexpr (kTabAsync) tab_slots = reinterpret_cast<float4*>(e3d_ring_smem);
   }
   // The PCG scalars live in shared memory: every thread reads them after a
   // barrier, thread 0 alone updates them (all blocks compute the same values
@@ -1883,7 +1933,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
       if constexpr (TMA)
         apply_tile_ring<E3D_RING_ZS>(A, t, sm, hAh_t, ring);
       else
-        apply_tile<T, true, (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), kDeferU>(A, t, sm, hAh_t);
+        apply_tile<T, true, (sizeof(T) == 4 && E3D_F32_POLD_SMEM != 0), kDeferU, kTabAsync>(A, t, sm, hAh_t,
+                                                                                           tab_slots);
       __syncthreads();
     }
     {

@@ -52,19 +52,16 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Scaled stiffness for phases 1..nphase at rows 1..nphase (row 0 unused), so the
-// 1-based phase ids of the caller index it directly.  Same arithmetic as
-// femat_phase_kernel.
+// Stiffness tables for phases 1..nphase at rows 1..nphase (row 0 unused), so the
+// 1-based phase ids of the caller index them directly.  Same arithmetic as
+// femat_phase_kernel (modal_table).
 __global__ void noalloc_table_kernel(const double* __restrict__ cmod, int nphase, double* __restrict__ table) {
   const int p = blockIdx.x;  // 0-based phase
-  for (int e = threadIdx.x; e < 36; e += blockDim.x) {
-    const int i = e / 6, j = e % 6;
-    const double c = cmod[p + (long long)nphase * (i + 6 * j)];
-    double* row = table + (long long)(p + 1) * kCsStride;
-    row[e] = c / 16.0;
-    row[36 + e] = c / 48.0;
-    row[72 + e] = c / 144.0;
-  }
+  if (threadIdx.x != 0) return;
+  double C6[6][6];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) C6[i][j] = cmod[p + (long long)nphase * (i + 6 * j)];
+  modal_table(C6, table + (long long)(p + 1) * kCsStride);
 }
 
 __global__ void noalloc_check_pix_kernel(const int32_t* __restrict__ pix, long long ns, int nphase,

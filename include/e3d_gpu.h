@@ -221,7 +221,7 @@ int32_t e3d_stencil_path(const e3d_handle_t* h);
  * and the scaled stiffness table and tile halos live in one static device
  * array of E3D_NOALLOC_SCRATCH_BYTES per GPU, held from library load to
  * process exit.  A grid whose scratch (about 41*3*ns/256 doubles of halos plus
- * 108*(nphase+1) doubles of table -- e.g. 128^3 with up to 4096 phases) does
+ * 126*(nphase+1) doubles of table -- e.g. 128^3 with up to 8600 phases) does
  * not fit is rejected with E3D_ERR_INPUT and e3d_last_cuda_error() says why.
  * Runs on `stream` (a cudaStream_t, NULL = legacy default) of the current
  * device; each call copies a phase-check flag back to host memory and waits
