@@ -138,5 +138,26 @@
             integer(c_int32_t), value :: n
             integer(c_int32_t), intent(out) :: cnt
           end function
+          ! HDF5 files without libhdf5 (include/e3d_micro.h): ppixel_hdf5 and the
+          ! fullfield_poly.h5 writer become two calls, so the Fortran driver
+          ! needs no HDF5 library.  Status 0, -1 I/O error, -2 bad or
+          ! unsupported file, -3 size mismatch, -4 phase id out of range.
+          integer(c_int32_t) function e3d_h5_micro_read(path, ns, ngrains, pix, rod) &
+              bind(C, name="e3d_h5_micro_read")
+            import :: c_int32_t, c_int64_t, c_double, c_char
+            character(kind=c_char), intent(in) :: path(*)
+            integer(c_int64_t), value :: ns
+            integer(c_int32_t), value :: ngrains
+            integer(c_int32_t), intent(out) :: pix(*)
+            real(c_double), intent(out) :: rod(*)
+          end function
+          integer(c_int32_t) function e3d_h5_fullfield_write(path, ns, pix, vm, sigma) &
+              bind(C, name="e3d_h5_fullfield_write")
+            import :: c_int32_t, c_int64_t, c_double, c_char
+            character(kind=c_char), intent(in) :: path(*)
+            integer(c_int64_t), value :: ns
+            integer(c_int32_t), intent(in) :: pix(*)
+            real(c_double), intent(in) :: vm(*), sigma(*)
+          end function
         end interface
       end module elas3d_gpu_mod
