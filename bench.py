@@ -484,8 +484,10 @@ def form_solve(args) -> dict:
     else:
         p, pix, rod = _workload(args.n)
     p.criterion = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
+    clocks = ClockSampler(p.device).start()
     a = _full_solve(e3d, p, pix, rod, e3d.PREC_FP64)
     b = _full_solve(e3d, p, pix, rod, e3d.PREC_MIXED)
+    clk = clocks.stop()
     err = abs(b["utot"] - a["utot"]) / abs(a["utot"])
     serr = float(((b["strav"] - a["strav"]) ** 2).sum() ** 0.5 / (a["strav"] ** 2).sum() ** 0.5)
     return {"metric": f"time to solution, {args.n}^3 (s)", "form": "solve", "unit": "s", "higher_is_better": False,
@@ -494,6 +496,7 @@ def form_solve(args) -> dict:
             "energy_rel_err_mixed_vs_fp64": err, "stress_rel_err_mixed_vs_fp64": serr,
             "energy": {"fp64": a["utot"], "mixed": b["utot"]},
             "criterion": args.criterion, "true_rel": {"fp64": a["true_rel"], "mixed": b["true_rel"]},
+            "clocks": clk,
             "config": {"workload": (f"c3_laguerre_{args.n}_A{args.zener:g}" if args.workload == "c3"
                                     else f"c2_polycrystal_{args.n}"),
                        "dof": 3 * p.ns, "grains": p.nphase - 1, "zener_A": 2.0 * p.c44 / (p.c11 - p.c12),
