@@ -529,7 +529,8 @@ def form_batch(args) -> dict:
     nodes = sum(int(np.prod(r["shape"])) for r in rves)
     t0 = time.perf_counter()
     crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
-    b = e3d.Batch(rves, max_iter=args.max_iter, criterion=crit, parts=args.parts, load_cases=args.load_cases)
+    b = e3d.Batch(rves, max_iter=args.max_iter, criterion=crit, parts=args.parts, load_cases=args.load_cases,
+                  refine_every=args.refine_every)
     t_create = time.perf_counter() - t0
     ceff, sec = b.solve()  # first solve
     clocks = ClockSampler(0).start()
@@ -571,7 +572,7 @@ def form_batch(args) -> dict:
             "speedup_vs_sequential_fp64": (nj / sec) / seq_rate if seq_rate else None,
             "config": {"workload": "ensemble", "rves": len(rves), "edges": "U{32..96}", "grains": "8-200",
                        "zener": "{0.5,0.75,1,1.5,2,3,4,5}", "pores": "0-2 %", "load_cases": 6,
-                       "launch": "one persistent launch from a CUDA graph"}}
+                       "launch": "one persistent launch from a CUDA graph", "refine_every": args.refine_every}}
 
 
 def form_serve(args) -> dict:
@@ -601,6 +602,7 @@ def form_serve(args) -> dict:
     budget = int(150e9)
     crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
     srv = e3d.Server(max_active=args.slots, round_iters=args.round_iters, max_iter=20000, hbm_budget=budget,
+                     refine_every=args.refine_every,
                      criterion=crit)
     clocks = ClockSampler(0).start()
     t0 = time.perf_counter()
@@ -666,7 +668,7 @@ def form_serve(args) -> dict:
                                                "for the solves before it"},
             "config": {"workload": "serve", "arrivals": f"Poisson, mean {args.rate}/s, seed 5",
                        "edges": f"U{{48..{args.serve_max_edge}}}", "grains": "16-1000", "zener": "U[0.5,5]",
-                       "pores": "0-3 %", "load": "one unit load case per request"}}
+                       "pores": "0-3 %", "load": "one unit load case per request", "refine_every": args.refine_every}}
 
 
 def main():
@@ -690,6 +692,9 @@ def main():
     ap.add_argument("--rve-edge", type=int, default=0, help="batch probe: equal RVEs of this edge (0: the ensemble)")
     ap.add_argument("--load-cases", type=int, default=0, help="batch: load-case bit mask (0: all six)")
     ap.add_argument("--max-iter", type=int, default=20000, help="batch: iteration cap per solve")
+    ap.add_argument("--refine-every", type=int, default=200,
+                    help="batch/serve: FP32 inner iterations between FP64 residual replacements (every solve "
+                         "still ends on an FP64 residual; batch at 50 / 100 / 200: 184 / 196 / 204 solves/s)")
     ap.add_argument("--requests", type=int, default=256, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=32, help="serve: concurrent solves")

@@ -3,13 +3,15 @@
 a fixed HBM budget).  Called through the C ABI with caller-owned device
 buffers, compared with the allocating entry point e3d_apply on the same
 problem, on two calls in a row (the second call finds the first call's
-contents in the shared static scratch).  Collected last on purpose."""
+contents in the shared static scratch), and the first result against the CPU
+oracle's K.x.  Collected last on purpose."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 import elas3d_xtal_gb300 as e3d
+import oracle as O
 from elas3d_xtal_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -56,6 +58,11 @@ def test_apply_noalloc_matches_apply_twice():
 
     assert call() == e3d.E3D_OK
     assert _rel(d_y.cpu().numpy(), y1_ref) < KU_TOL
+    # and against the CPU oracle's K.x (the reference's stencil, restated)
+    s = p.strain
+    op = O.Problem(p.nx, p.ny, p.nz, p.nphase, c11=p.c11, c12=p.c12, c44=p.c44, exx=s[0], eyy=s[1], ezz=s[2],
+                   exz=s[3], eyz=s[4], exy=s[5])
+    assert _rel(d_y.cpu().numpy(), O.Oracle(op, pix, rod).femat().apply(x1)) < KU_TOL
     free_before = torch.cuda.mem_get_info(0)[0]
     d_x.copy_(torch.from_numpy(x2).to(dev))
     d_y.fill_(float("nan"))
