@@ -658,14 +658,14 @@ def form_serve(args) -> dict:
                      "iterations": {"min": int(min(r["iterations"] for r in res)),
                                     "max": int(max(r["iterations"] for r in res)),
                                     "mean": float(np.mean([r["iterations"] for r in res]))}},
-            "sequential_fp64": {"sample": m, "solves_per_s": m / sum(seq),
-                                "energy_rel_err_vs_served": {"max": max(errs), "median": float(np.median(errs))},
-                                "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
-                                              "p99": float(np.percentile(seq_lat, 99))},
-                                "served_latency_same_requests_s": {"p50": float(np.percentile(served_lat, 50)),
-                                                                   "p99": float(np.percentile(served_lat, 99))},
-                                "queue_model": "each sampled request arrives at its own Poisson time and waits "
-                                               "for the solves before it"},
+            "sequential_fp64": ({"sample": m, "solves_per_s": m / sum(seq),
+                                 "energy_rel_err_vs_served": {"max": max(errs), "median": float(np.median(errs))},
+                                 "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
+                                               "p99": float(np.percentile(seq_lat, 99))},
+                                 "served_latency_same_requests_s": {"p50": float(np.percentile(served_lat, 50)),
+                                                                    "p99": float(np.percentile(served_lat, 99))},
+                                 "queue_model": "each sampled request arrives at its own Poisson time and waits "
+                                                "for the solves before it"} if m else {"sample": 0}),
             "config": {"workload": "serve", "arrivals": f"Poisson, mean {args.rate}/s, seed 5",
                        "edges": f"U{{48..{args.serve_max_edge}}}", "grains": "16-1000", "zener": "U[0.5,5]",
                        "pores": "0-3 %", "load": "one unit load case per request", "refine_every": args.refine_every}}
