@@ -693,8 +693,9 @@ def main():
     ap.add_argument("--load-cases", type=int, default=0, help="batch: load-case bit mask (0: all six)")
     ap.add_argument("--max-iter", type=int, default=20000, help="batch: iteration cap per solve")
     ap.add_argument("--refine-every", type=int, default=200,
-                    help="batch/serve: FP32 inner iterations between FP64 residual replacements (every solve "
-                         "still ends on an FP64 residual; batch at 50 / 100 / 200: 184 / 196 / 204 solves/s)")
+                    help="batch/serve: FP32 inner iterations between FP64 residual replacements at most (the "
+                         "engine also replaces after a 1e-3 residual drop, and every solve ends on an FP64 "
+                         "residual; batch at 50 / 100 / 200: 184 / 196 / 204 solves/s)")
     ap.add_argument("--requests", type=int, default=256, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=32, help="serve: concurrent solves")

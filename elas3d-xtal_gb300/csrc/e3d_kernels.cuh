@@ -1777,6 +1777,7 @@ __device__ void flush_u_tiles(const GridDims& G, long long first, long long stri
 //      rel_res, divergence reset (:1961-1981), gamma (:1988), stop test (:2007)
 struct PcgState {
   double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
+  double rel_at_replace;  // job engine: rel_res of the last FP64 residual (set-up or replacement)
   int it, status, reset, resets, cur, max_iter, divergence_reset, refinements;
   int since_replace, final_ready;  // final_ready: the job engine ended on a converged FP64 replacement
 };
