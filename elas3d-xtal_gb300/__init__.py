@@ -82,7 +82,7 @@ class ProblemC(C.Structure):
         ("flag_m", C.c_int32), ("criterion", C.c_int32), ("precision", C.c_int32),
         ("divergence_reset", C.c_int32), ("max_iter", C.c_int32), ("device", C.c_int32),
         ("tol", C.c_float), ("refine_every", C.c_int32),
-        ("preconditioner", C.c_int32), ("reserved", C.c_int32),
+        ("preconditioner", C.c_int32), ("refine_decades", C.c_int32),
         ("c11", C.c_double), ("c12", C.c_double), ("c44", C.c_double),
         ("e1", C.c_double), ("nu1", C.c_double), ("strain", C.c_double * 6),
         ("hbm_budget", C.c_int64),
@@ -239,6 +239,7 @@ class Problem:
     divergence_reset: int = 1
     refine_every: int = 0
     preconditioner: int = PRECOND_BLOCK_JACOBI
+    refine_decades: int = 0  # MIXED: also replace after this many decades of FP32 residual drop
     device: int = 0
     hbm_budget: int = 0
 
@@ -252,7 +253,7 @@ class Problem:
         p.flag_m, p.criterion, p.precision = self.flag_m, self.criterion, self.precision
         p.divergence_reset, p.max_iter, p.device = self.divergence_reset, self.max_iter, self.device
         p.tol, p.refine_every = self.tol, self.refine_every
-        p.preconditioner, p.reserved = self.preconditioner, 0
+        p.preconditioner, p.refine_decades = self.preconditioner, self.refine_decades
         p.c11, p.c12, p.c44, p.e1, p.nu1 = self.c11, self.c12, self.c44, self.e1, self.nu1
         for i in range(6):
             p.strain[i] = float(self.strain[i])

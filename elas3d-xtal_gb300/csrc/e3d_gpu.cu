@@ -320,6 +320,7 @@ int32_t e3d_create(e3d_handle_t** out, const e3d_problem_t* p) {
   if (p->precision != E3D_PREC_FP64 && p->precision != E3D_PREC_MIXED) return E3D_ERR_INPUT;
   if (p->criterion != E3D_CRIT_REF && p->criterion != E3D_CRIT_PRECOND_REL) return E3D_ERR_INPUT;
   if (p->preconditioner != E3D_PRECOND_BLOCK_JACOBI && p->preconditioner != E3D_PRECOND_NONE) return E3D_ERR_INPUT;
+  if (p->refine_decades < 0 || p->refine_decades > 15) return E3D_ERR_INPUT;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
@@ -587,8 +588,11 @@ int32_t e3d_solve_begin(e3d_handle_t* h) {
     pcg_init_kernel<double><<<grid, 256, 0, h->stream>>>(h->G, h->minv, h->g, h->z, h->partial);
   }
   E3D_LAUNCHED(h);
+  const double drop = (h->prob.precision == E3D_PREC_MIXED && h->prob.refine_decades > 0)
+                         ? std::pow(10.0, -(double)h->prob.refine_decades)
+                         : 0.0;
   pcg_init_scalars_kernel<<<1, 256, 0, h->stream>>>(h->partial, grid, h->gg0, h->prob.criterion, h->prob.tol,
-                                                    h->prob.max_iter, h->prob.divergence_reset, h->st);
+                                                    h->prob.max_iter, h->prob.divergence_reset, drop, h->st);
   E3D_LAUNCHED(h);
   E3D_CUDA(cudaEventRecord(e1, h->stream));
   int32_t rc = sync(h);
@@ -751,23 +755,27 @@ int32_t e3d_iterate(e3d_handle_t* h, int32_t n, e3d_solve_stats_t* st) {
   int remaining = n;
   int32_t rc = E3D_OK;
   PcgState S{};
-  while (remaining > 0) {
+  if ((rc = read_state(h, &S))) remaining = 0;
+  while (remaining > 0 && S.status == PCG_RUNNING) {
     int chunk = std::min(remaining, 256);
     if (mixed) chunk = std::min(chunk, R - h->since_replace);
+    const int it0 = S.it;
     rc = mixed ? launch_pcg<float>(h, chunk) : launch_pcg<double>(h, chunk);
     if (rc) break;
     if ((rc = read_state(h, &S))) break;
-    const int done = S.it;  // iterations so far
-    (void)done;
-    remaining -= chunk;
+    // a launch ends early when the solve stops or, in the mixed form with
+    // refine_decades set, when the FP32 residual calls for a replacement
+    const int done = S.it - it0;
+    remaining -= done;
     if (mixed) {
-      h->since_replace += chunk;
-      if (S.status == PCG_CONVERGED || (S.status == PCG_RUNNING && h->since_replace >= R)) {
+      h->since_replace += done;
+      if (S.status == PCG_CONVERGED || S.status == PCG_REPLACE ||
+          (S.status == PCG_RUNNING && h->since_replace >= R)) {
         if ((rc = residual_replacement(h))) break;
         if ((rc = read_state(h, &S))) break;
       }
     }
-    if (S.status != PCG_RUNNING) break;
+    if (done == 0 && S.status == PCG_RUNNING) break;  // nothing advanced: do not spin
   }
   if (!rc && mixed) rc = fold_correction(h);  // u always holds the current iterate on return
   cudaEventRecord(e1, h->stream);

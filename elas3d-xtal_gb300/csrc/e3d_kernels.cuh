@@ -91,7 +91,15 @@ constexpr int NT = TILE_X * TILE_Y;  // threads per block of the tile kernels
 // Device status codes (host maps them to E3D_*).
 enum : int { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_BAD_INDEX = 2 };
 // PCG status.
-enum : int { PCG_RUNNING = 0, PCG_CONVERGED = 1, PCG_HAH = 2, PCG_MAXITER = 3, PCG_BREAKDOWN = 4, PCG_TIMEOUT = 5 };
+enum : int {
+  PCG_RUNNING = 0,
+  PCG_CONVERGED = 1,
+  PCG_HAH = 2,
+  PCG_MAXITER = 3,
+  PCG_BREAKDOWN = 4,
+  PCG_TIMEOUT = 5,
+  PCG_REPLACE = 6  // mixed form: the FP32 residual has dropped far enough for an FP64 replacement
+};
 
 struct GridDims {
   int nx, ny, nz;
@@ -1777,7 +1785,8 @@ __device__ void flush_u_tiles(const GridDims& G, long long first, long long stri
 //      rel_res, divergence reset (:1961-1981), gamma (:1988), stop test (:2007)
 struct PcgState {
   double gg, gg0, rel_res_prev, gamma, rel_res, tol, hAh, gglast;
-  double rel_at_replace;  // job engine: rel_res of the last FP64 residual (set-up or replacement)
+  double rel_at_replace;  // mixed form: rel_res of the last FP64 residual (set-up or replacement)
+  double refine_drop;     // mixed form: replace once rel_res < refine_drop * rel_at_replace (0: never)
   int it, status, reset, resets, cur, max_iter, divergence_reset, refinements;
   int since_replace, final_ready;  // final_ready: the job engine ended on a converged FP64 replacement
 };
@@ -2005,7 +2014,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (TMA && E3D_RING_ZS == 2 
           s.reset = 0;
         }
         s.rel_res_prev = rel_res;
-        if (rel_res < s.tol) s.status = PCG_CONVERGED;
+        if (rel_res < s.tol)
+          s.status = PCG_CONVERGED;
+        else if (sizeof(T) == 4 && s.refine_drop > 0.0 && rel_res < s.refine_drop * s.rel_at_replace)
+          s.status = PCG_REPLACE;  // the host replaces the residual in FP64 and relaunches
       }
     }
     __syncthreads();
@@ -2044,7 +2056,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(GridDims G, const T* __re
 
 static __global__ void pcg_init_scalars_kernel(const double* __restrict__ partial, int n, double gg0_ref,
                                         int criterion, float tol, int max_iter, int divergence_reset,
-                                        PcgState* st) {
+                                        double refine_drop, PcgState* st) {
   __shared__ double red[8];
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
@@ -2069,6 +2081,8 @@ static __global__ void pcg_init_scalars_kernel(const double* __restrict__ partia
     S.refinements = 0;
     S.since_replace = 0;
     S.final_ready = 0;
+    S.rel_at_replace = S.rel_res_prev;
+    S.refine_drop = refine_drop;
     *st = S;
   }
 }
@@ -2135,12 +2149,14 @@ static __global__ void replace_scalars_kernel(const double* __restrict__ partial
     PcgState S = *st;
     S.gg = gg;
     S.refinements += 1;
+    if (S.status == PCG_REPLACE) S.status = PCG_RUNNING;
     if (!isfinite(gg)) {
       S.status = PCG_BREAKDOWN;
     } else {
       const double rel = sqrt(gg / S.gg0);
       S.rel_res = rel;
       S.rel_res_prev = rel;
+      S.rel_at_replace = rel;
       if (!S.reset) S.gamma = gg / S.gglast;
       if (history && S.it > 0) history[E3D_IDX(S.it - 1, S.max_iter)] = rel;
       if (S.status == PCG_CONVERGED && !(rel < S.tol)) S.status = PCG_RUNNING;

@@ -30,7 +30,7 @@
           integer(c_int32_t) :: max_iter, device
           real(c_float)      :: tol
           integer(c_int32_t) :: refine_every
-          integer(c_int32_t) :: preconditioner, reserved
+          integer(c_int32_t) :: preconditioner, refine_decades
           real(c_double)     :: c11, c12, c44, e1, nu1
           real(c_double)     :: strain(6)      ! exx eyy ezz exz eyz exy (tensor)
           integer(c_int64_t) :: hbm_budget

@@ -76,7 +76,8 @@ typedef struct e3d_problem {
   float tol;                /* single precision, as `real :: tol` (:148)           */
   int32_t refine_every;     /* MIXED: FP64 residual replacement period (0 = 50)    */
   int32_t preconditioner;   /* E3D_PRECOND_*                                       */
-  int32_t reserved;         /* zero                                                */
+  int32_t refine_decades;   /* MIXED: also replace once the FP32 residual has fallen
+                               this many decades below the last FP64 one (0: never) */
   double c11, c12, c44;     /* cubic constants, Pa (:100-102)                      */
   double e1, nu1;           /* inclusion Young's modulus / Poisson ratio (:114-115)*/
   double strain[6];         /* exx, eyy, ezz, exz, eyz, exy (tensor) (:394-399)    */

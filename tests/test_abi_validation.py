@@ -25,9 +25,10 @@ def _create(L, **kw):
 
 @pytest.mark.parametrize("kw", [dict(nx=0), dict(ny=-1), dict(nz=0), dict(nphase=0), dict(max_iter=-1),
                                 dict(precision=7), dict(criterion=9), dict(preconditioner=5),
-                                dict(nx=1 << 14, ny=1 << 14, nz=1 << 13)],
+                                dict(nx=1 << 14, ny=1 << 14, nz=1 << 13), dict(refine_decades=-1),
+                                dict(refine_decades=16)],
                          ids=["nx0", "ny-1", "nz0", "nphase0", "max_iter-1", "precision", "criterion",
-                              "preconditioner", "over-2^40-nodes"])
+                              "preconditioner", "over-2^40-nodes", "refine_decades-1", "refine_decades16"])
 def test_create_rejects_bad_problems(L, kw):
     rc, h = _create(L, **kw)
     assert rc == e3d.E3D_ERR_INPUT

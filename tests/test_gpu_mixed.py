@@ -106,3 +106,32 @@ def test_handle_reused_after_breakdown_ignores_stale_directions():
     assert r2["exit_reason"] == e3d.EXIT_CONVERGED
     assert r2["iterations"] == r1["iterations"]
     assert np.array_equal(u1, u2)
+
+
+@pytest.mark.parametrize("criterion", [e3d.CRIT_REF, e3d.CRIT_PRECOND_REL])
+def test_mixed_replacement_on_residual_drop(criterion):
+    """refine_decades: an FP64 replacement whenever the FP32 residual has fallen
+    three decades below the last FP64 one, with the fixed period out of the way
+    (1000).  The solve still ends on an FP64 residual and meets the FP64 oracle,
+    with fewer replacements than one every 50 iterations."""
+    p, pix, rod = W.c2(n=24)
+    p.criterion = criterion
+    p.precision = e3d.PREC_MIXED
+    ref = O.run(_oracle_problem(p), pix, rod)
+    p.refine_every = 50
+    with e3d.Elas3D(p) as g:
+        g.upload(pix, rod)
+        fixed = g.run()
+    p.refine_every, p.refine_decades = 1000, 3
+    with e3d.Elas3D(p) as g:
+        g.upload(pix, rod)
+        res = g.run()
+    assert res["exit_reason"] == e3d.EXIT_CONVERGED
+    assert res["rel_res"] < p.tol
+    assert abs(res["iterations"] - fixed["iterations"]) <= 3
+    assert 1 <= res["refinements"] <= fixed["refinements"]
+    tol = ENERGY_TOL * abs(ref["utot"])
+    if criterion == e3d.CRIT_REF:  # the reference's loose stop: see test_gpu_parity_configs.py
+        p.criterion = e3d.CRIT_PRECOND_REL
+        tol = max(tol, 0.01 * abs(ref["utot"] - O.run(_oracle_problem(p), pix, rod)["utot"]))
+    assert abs(res["utot"] - ref["utot"]) <= tol
