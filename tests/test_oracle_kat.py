@@ -273,3 +273,34 @@ def test_pcg_in_steps_equals_dembx():
     d = s.close()
     assert d["lstep"] == r["lstep"] and d["reason"] == r["reason"] == 0
     assert np.array_equal(s.u, r["u"]) and np.array_equal(d["history"], r["history"])
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_laminate_matches_the_closed_form(axis):
+    """A laminate of rotated cubic grains (tests/analytic.py): the converged
+    solve carries the closed-form energy, <sigma> and <eps> to rounding, and
+    an unconverged iterate (the reference's stop test) lies above the exact
+    energy, which is the minimum."""
+    import analytic as AN
+
+    rng = np.random.default_rng(50 + axis)
+    shape = [(12, 5, 6), (5, 11, 4), (6, 5, 13)][axis]
+    ng = 4
+    layers = rng.integers(1, ng + 1, size=shape[axis])
+    pix = AN.laminate_pix(shape, layers, axis)
+    rod = rng.normal(size=3 * ng)
+    s = np.array([1e-3, -3e-4, 2e-4, 4e-4, -2e-4, 3e-4])
+    c11, c12, c44 = (v * 1e9 for v in A_SWEEP[3.0])
+    for crit in (1, 0):
+        p = O.Problem(*shape, ng + 1, c11=c11, c12=c12, c44=c44, exx=s[0], eyy=s[1], ezz=s[2], exz=s[3],
+                      eyz=s[4], exy=s[5], tol=1e-10, criterion=crit)
+        r = O.run(p, pix, rod)
+        cm = O.Oracle(p, pix, rod).femat().cmod_array()
+        w, sig, _ = AN.laminate_exact(cm, layers, AN.engineering(s), axis)
+        assert r["exit_reason"] == 0
+        assert _rel(r["epsav"], AN.engineering(s)) < 1e-13
+        if crit == 1:
+            assert abs(r["utot"] - w * p.ns) <= 1e-12 * w * p.ns
+            assert _rel(r["strav"], sig) < 1e-12
+        else:
+            assert 0 <= r["utot"] - w * p.ns <= 1e-8 * w * p.ns
