@@ -197,6 +197,63 @@ static __device__ __noinline__ double job_c_elem(const JobDesc& J, int x, int y,
   return 0.5 * e;
 }
 
+// Boundary nodes (x, y or z on a face of the box), each once: the two x faces
+// whole, then the y faces at interior x, then the z faces at interior x and y.
+// Consecutive indices are consecutive x where the set allows, so a warp's
+// lanes share the work of job_b_node instead of idling beside one boundary lane.
+__device__ __forceinline__ long long boundary_node_count(const GridDims& G) {
+  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1, fz = G.nz > 1 ? 2 : 1;
+  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
+  return fx * G.ny * G.nz + ix * fy * G.nz + ix * iy * fz;
+}
+
+__device__ __forceinline__ void boundary_node(const GridDims& G, long long t, int& x, int& y, int& z) {
+  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1;
+  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
+  const long long na = fx * G.ny * G.nz, nb = ix * fy * G.nz;
+  if (t < na) {
+    const long long r = t / fx;
+    x = (t % fx) == 0 ? 0 : G.nx - 1;
+    y = (int)(r % G.ny);
+    z = (int)(r / G.ny);
+  } else if (t < na + nb) {
+    const long long s = t - na, r = s / ix;
+    x = 1 + (int)(s % ix);
+    y = (r % fy) == 0 ? 0 : G.ny - 1;
+    z = (int)(r / fy);
+  } else {
+    const long long s = t - na - nb, r = s / ix;
+    x = 1 + (int)(s % ix);
+    y = 1 + (int)(r % iy);
+    z = (r / iy) == 0 ? 0 : G.nz - 1;
+  }
+}
+
+// Elements with a corner across a high face (i = nx-1, j = ny-1 or k = nz-1),
+// each once, as femat_c_kernel enumerates them.
+__device__ __forceinline__ long long boundary_element_count(const GridDims& G) {
+  return (long long)G.ny * G.nz + (long long)(G.nx - 1) * G.nz + (long long)(G.nx - 1) * (G.ny - 1);
+}
+
+__device__ __forceinline__ void boundary_element(const GridDims& G, long long t, int& i, int& j, int& k) {
+  const long long nfx = (long long)G.ny * G.nz, nfy = (long long)(G.nx - 1) * G.nz;
+  if (t < nfx) {
+    i = G.nx - 1;
+    j = (int)(t % G.ny);
+    k = (int)(t / G.ny);
+  } else if (t < nfx + nfy) {
+    const long long s = t - nfx;
+    j = G.ny - 1;
+    i = (int)(s % (G.nx - 1));
+    k = (int)(s / (G.nx - 1));
+  } else {
+    const long long s = t - nfx - nfy;
+    k = G.nz - 1;
+    i = (int)(s % (G.nx - 1));
+    j = (int)(s / (G.nx - 1));
+  }
+}
+
 template <typename T>
 __device__ ApplyArgs<T> job_apply_args(const JobDesc& J);
 
@@ -409,18 +466,34 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       const double exx = J.J.E[0][0], eyy = J.J.E[1][1], ezz = J.J.E[2][2];
       const double exy = J.J.E[0][1], exz = J.J.E[0][2], eyz = J.J.E[1][2];
       for_part_nodes(J, part, [&](long long m, int x, int y, int z, int, int, int, int, int, int) {
-        double bb[3];
-        job_b_node(J, x, y, z, bb);
-        J.b[m] = bb[0];
-        J.b[m + ns] = bb[1];
-        J.b[m + 2 * ns] = bb[2];
-        cpart += job_c_elem(J, x, y, z);
+        if (!(x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1))
+          J.b[m] = J.b[m + ns] = J.b[m + 2 * ns] = 0.0;  // boundary nodes: below
         const double xd = x, yd = y, zd = z;
         J.u[m] = xd * exx + yd * exy + zd * exz;
         J.u[m + ns] = xd * exy + yd * eyy + zd * eyz;
         J.u[m + 2 * ns] = xd * exz + yd * eyz + zd * ezz;
         J.du[m] = J.du[m + ns] = J.du[m + 2 * ns] = 0.0f;
       });
+      // b at the boundary nodes and C over the boundary elements, both listed
+      // compactly and shared by all threads of all parts
+      const long long stride = (long long)J.nparts * NT, first = (long long)part * NT + threadIdx.x;
+      const long long nbn = boundary_node_count(G);
+      for (long long t = first; t < nbn; t += stride) {
+        int x, y, z;
+        boundary_node(G, t, x, y, z);
+        double bb[3];
+        job_b_node(J, x, y, z, bb);
+        const long long m = E3D_IDX((long long)x + (long long)G.nx * y + (long long)G.nx * G.ny * z, ns);
+        J.b[m] = bb[0];
+        J.b[m + ns] = bb[1];
+        J.b[m + 2 * ns] = bb[2];
+      }
+      const long long nbe = boundary_element_count(G);
+      for (long long t = first; t < nbe; t += stride) {
+        int i, j, k;
+        boundary_element(G, t, i, j, k);
+        cpart += job_c_elem(J, i, j, k);
+      }
       job_put(J, SL_C, part, cpart, red);
       ok = job_barrier(J.bar, J.nparts, E.err, to);
       if (ok) ok = job_fp64_apply_u(J, part, sm64, E.err, to);
