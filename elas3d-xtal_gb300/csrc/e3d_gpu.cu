@@ -442,24 +442,31 @@ int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rod) {
   const auto& p = h->prob;
   if (p.flag_m == 1 && p.nphase > 1 && !rod) return E3D_ERR_INPUT;
   const long long ns = h->G.ns;
-  // phase range check (ppixel_hdf5, src/elas3dxtal_pcg.f90:2986-2989) and
-  // conversion to 0-based ids.
-  std::vector<int32_t> p0((size_t)ns);
-  for (long long m = 0; m < ns; ++m) {
-    const int32_t v = pix[m];
-    if (v < 1 || v > p.nphase) return E3D_ERR_INPUT;
-    p0[(size_t)m] = v - 1;
-  }
   cudaSetDevice(h->device);
-  E3D_CUDA(cudaMemcpyAsync(h->pix, p0.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, h->stream));
+  // The ids go to the device as they are (one DMA from the caller's buffer,
+  // at full speed when it is pinned); the phase range check (ppixel_hdf5,
+  // src/elas3dxtal_pcg.f90:2986-2989) and the conversion to 0-based ids run
+  // there, over the whole map in one pass.  A refused map leaves the handle
+  // without an upload.
+  h->uploaded = false;
+  h->femat_done = h->energy_done = h->solve_ready = h->minv_ready = false;
+  E3D_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  E3D_CUDA(cudaMemcpyAsync(h->pix, pix, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, h->stream));
+  pix_to_zero_based_kernel<<<blocks_for(ns, 256), 256, 0, h->stream>>>(ns, p.nphase, h->pix, h->err);
+  E3D_LAUNCHED(h);
   if (rod && p.nphase > 1)
     E3D_CUDA(cudaMemcpyAsync(h->rod, rod, sizeof(double) * 3 * (p.nphase - 1), cudaMemcpyHostToDevice, h->stream));
   else
     E3D_CUDA(cudaMemsetAsync(h->rod, 0, sizeof(double) * 3, h->stream));
-  int32_t rc = sync(h);
-  if (rc) return rc;
+  E3D_CUDA(cudaStreamSynchronize(h->stream));
+  int derr = 0;
+  E3D_CUDA(cudaMemcpy(&derr, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (derr != DEV_OK) {
+    E3D_CUDA(cudaMemset(h->err, 0, sizeof(int)));
+    e3d_record_error_text("e3d_upload: a phase id lies outside [1, nphase]");
+    return E3D_ERR_INPUT;
+  }
   h->uploaded = true;
-  h->femat_done = h->energy_done = h->solve_ready = h->minv_ready = false;
   return E3D_OK;
 }
 

@@ -112,8 +112,10 @@ int32_t e3d_create(e3d_handle_t** h, const e3d_problem_t* p);
 int32_t e3d_destroy(e3d_handle_t* h);
 
 /* Phase map + orientations, as read by ppixel_hdf5 (:2879-2990): pix has ns
- * entries in [1, nphase] (checked as at :2986-2989), rodrigues has
- * 3*(nphase-1) entries (ignored when flag_m == 0, may be NULL then). */
+ * entries in [1, nphase] (checked as at :2986-2989, on the device after one
+ * copy of the map; a pinned pix buffer copies fastest), rodrigues has
+ * 3*(nphase-1) entries (ignored when flag_m == 0, may be NULL then).  On
+ * E3D_ERR_INPUT the handle holds no phase map until the next upload. */
 int32_t e3d_upload(e3d_handle_t* h, const int32_t* pix, const double* rodrigues);
 
 /* e3d_upload with the phase map already in device memory (d_pix: ns int32 on

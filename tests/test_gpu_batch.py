@@ -78,3 +78,28 @@ def test_batch_load_case_mask_and_budget(small_ensemble):
     with pytest.raises(e3d.E3DError) as ei:
         e3d.Batch(small_ensemble, hbm_budget=1 << 20)
     assert ei.value.code == e3d.E3D_ERR_OOM
+
+
+def test_batch_thin_rves_match_oracle():
+    """RVEs one and two nodes thick in some direction: every node is a boundary
+    node there, and the engine's boundary lists (b at boundary nodes, C over the
+    elements across the high faces) must cover each exactly once."""
+    shapes = [(1, 7, 6), (2, 6, 5), (7, 1, 4), (5, 6, 2), (2, 2, 3)]
+    rves = [W.rve(0, 3, 30 + i, A=2.5, shape=s) for i, s in enumerate(shapes)]
+    with e3d.Batch(rves, criterion=e3d.CRIT_PRECOND_REL, tol=1e-9) as b:
+        b.solve()
+        res = b.results()
+    assert len(res) == 6 * len(rves)
+    for r in res:
+        assert r["status"] == e3d.EXIT_CONVERGED, r
+        rve = rves[r["rve"]]
+        s = [0.0] * 6
+        s[r["load_case"]] = 1e-3 if r["load_case"] < 3 else 0.5e-3
+        nx, ny, nz = rve["shape"]
+        p = O.Problem(nx, ny, nz, rve["ngrains"] + 1, c11=rve["c11"], c12=rve["c12"], c44=rve["c44"],
+                      exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5], tol=1e-9, criterion=1)
+        ref = O.run(p, rve["pix"], rve["rodrigues"])
+        assert ref["exit_reason"] == 0
+        assert abs(r["utot0"] - ref["utot0"]) <= 1e-12 * abs(ref["utot0"])
+        assert abs(r["utot"] - ref["utot"]) <= ENERGY_TOL * abs(ref["utot"])
+        assert np.linalg.norm(r["strav"] - ref["strav"]) <= STRESS_TOL * np.linalg.norm(ref["strav"])

@@ -105,7 +105,8 @@ def workload(check):
     assert rc == e3d.E3D_OK
     out["noalloc"] = (0, float(torch.linalg.norm(d_y).item()))
     check("noalloc")
-    rves = [W.rve(12, 4, 5, A=2.0), W.rve(0, 6, 6, A=0.5, pore_frac=0.02, shape=(20, 9, 14))]
+    rves = [W.rve(12, 4, 5, A=2.0), W.rve(0, 6, 6, A=0.5, pore_frac=0.02, shape=(20, 9, 14)),
+            W.rve(0, 3, 7, A=2.5, shape=(1, 7, 6)), W.rve(0, 2, 8, A=3.0, shape=(2, 2, 3))]
     for parts in (0, 3):
         with e3d.Batch(rves, parts=parts) as b:
             ceff, _ = b.solve()

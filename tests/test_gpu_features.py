@@ -116,3 +116,26 @@ def test_driver_end_to_end(tmp_path, fmt):
     den = np.linalg.norm(sig_ref)
     assert np.linalg.norm(sig.ravel() - sig_ref) <= 1e-6 * den  # the converged fields of two solvers
     assert np.linalg.norm(e3d.h5_read(ff, "vm") - vm_ref) <= 1e-6 * np.linalg.norm(vm_ref)
+
+
+def test_upload_refuses_out_of_range_phases_and_recovers():
+    """The phase range check (src/elas3dxtal_pcg.f90:2986-2989) runs on the
+    device after one copy of the map: a refused map leaves no upload behind
+    (femat refuses), and a correct upload afterwards solves like a fresh one."""
+    p, pix, rod = W.c1(n=10, ngrains=4, seed=3)
+    with e3d.Elas3D(p) as g:
+        for bad_value in (0, p.nphase + 1):
+            bad = pix.copy()
+            bad[p.ns // 2] = bad_value
+            with pytest.raises(e3d.E3DError) as ei:
+                g.upload(bad, rod)
+            assert ei.value.code == e3d.E3D_ERR_INPUT
+            with pytest.raises(e3d.E3DError) as ei:
+                g.femat()
+            assert ei.value.code == e3d.E3D_ERR_STATE
+        g.upload(pix, rod)
+        res = g.run()
+    with e3d.Elas3D(p) as g2:
+        g2.upload(pix, rod)
+        ref = g2.run()
+    assert res["iterations"] == ref["iterations"] and res["utot"] == ref["utot"]
