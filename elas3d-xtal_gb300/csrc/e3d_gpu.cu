@@ -523,7 +523,9 @@ int32_t e3d_femat(e3d_handle_t* h) {
   }
   femat_phase_kernel<<<p.nphase, 32, 0, h->stream>>>(P, h->rod, h->cmod, h->cs, h->cs32, h->dk, h->dkd);
   E3D_LAUNCHED(h);
-  femat_b_kernel<<<blocks_for(h->G.ns, 256), 256, 0, h->stream>>>(h->G, h->J, h->pix, h->dk, h->b);
+  E3D_CUDA(cudaMemsetAsync(h->b, 0, sizeof(double) * 3 * h->G.ns, h->stream));  // interior nodes
+  femat_b_kernel<<<blocks_for(boundary_node_count(h->G), 256), 256, 0, h->stream>>>(h->G, h->J, h->pix, h->dk,
+                                                                                         h->b);
   E3D_LAUNCHED(h);
   const int grid = reduction_grid(h);
   femat_c_kernel<<<grid, 256, 0, h->stream>>>(h->G, h->J, h->pix, h->dk, h->partial);

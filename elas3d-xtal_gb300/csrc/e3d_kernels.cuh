@@ -1255,32 +1255,64 @@ __device__ __forceinline__ void element_delta(const GridDims& G, const JumpParam
   }
 }
 
+// Boundary nodes (x, y or z on a face of the box), each once: the two x faces
+// whole, then the y faces at interior x, then the z faces at interior x and y.
+// Consecutive indices are consecutive x where the set allows, so a warp's
+// lanes share the boundary work instead of idling beside one boundary lane.
+__host__ __device__ inline long long boundary_node_count(const GridDims& G) {
+  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1, fz = G.nz > 1 ? 2 : 1;
+  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
+  return fx * G.ny * G.nz + ix * fy * G.nz + ix * iy * fz;
+}
+
+__device__ __forceinline__ void boundary_node(const GridDims& G, long long t, int& x, int& y, int& z) {
+  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1;
+  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
+  const long long na = fx * G.ny * G.nz, nb = ix * fy * G.nz;
+  if (t < na) {
+    const long long r = t / fx;
+    x = (t % fx) == 0 ? 0 : G.nx - 1;
+    y = (int)(r % G.ny);
+    z = (int)(r / G.ny);
+  } else if (t < na + nb) {
+    const long long s = t - na, r = s / ix;
+    x = 1 + (int)(s % ix);
+    y = (r % fy) == 0 ? 0 : G.ny - 1;
+    z = (int)(r / fy);
+  } else {
+    const long long s = t - na - nb, r = s / ix;
+    x = 1 + (int)(s % ix);
+    y = 1 + (int)(r % iy);
+    z = (r / iy) == 0 ? 0 : G.nz - 1;
+  }
+}
+
+// b over the boundary nodes listed by boundary_node (b is zero elsewhere and
+// cleared beforehand): one thread per boundary node.
 static __global__ void femat_b_kernel(GridDims G, JumpParams J, const int32_t* __restrict__ pix,
                                const double* __restrict__ dk, double* __restrict__ b) {
-  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= G.ns) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= boundary_node_count(G)) return;
   int x, y, z;
-  node_xyz(G, m, x, y, z);
+  boundary_node(G, t, x, y, z);
+  const long long m = E3D_IDX((long long)x + (long long)G.nx * y + (long long)G.nx * G.ny * z, G.ns);
   double acc[3] = {0.0, 0.0, 0.0};
-  const bool edge = (x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1);
-  if (edge) {
-    // elements containing m in reference order 27,7,6,5,25,15,14,13 (local node ra)
-    for (int ra = 0; ra < 8; ++ra) {
-      const int a = kRefToCorner[ra];
-      const int ex = wrapi(x - (a & 1), G.nx), ey = wrapi(y - ((a >> 1) & 1), G.ny),
-                ez = wrapi(z - ((a >> 2) & 1), G.nz);
-      double d[8][3];
-      bool any;
-      element_delta(G, J, ex, ey, ez, d, any);
-      if (!any) continue;
-      const int ph = pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
-      const double* D = dk + (long long)ph * 576;
-      for (int i = 0; i < 3; ++i) {
-        double s = 0.0;
-        for (int rb = 0; rb < 8; ++rb)
-          for (int jj = 0; jj < 3; ++jj) s += D[(ra * 3 + i) * 24 + rb * 3 + jj] * d[rb][jj];
-        acc[i] += s;
-      }
+  // elements containing m in reference order 27,7,6,5,25,15,14,13 (local node ra)
+  for (int ra = 0; ra < 8; ++ra) {
+    const int a = kRefToCorner[ra];
+    const int ex = wrapi(x - (a & 1), G.nx), ey = wrapi(y - ((a >> 1) & 1), G.ny),
+              ez = wrapi(z - ((a >> 2) & 1), G.nz);
+    double d[8][3];
+    bool any;
+    element_delta(G, J, ex, ey, ez, d, any);
+    if (!any) continue;
+    const int ph = pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
+    const double* D = dk + (long long)ph * 576;
+    for (int i = 0; i < 3; ++i) {
+      double s = 0.0;
+      for (int rb = 0; rb < 8; ++rb)
+        for (int jj = 0; jj < 3; ++jj) s += D[(ra * 3 + i) * 24 + rb * 3 + jj] * d[rb][jj];
+      acc[i] += s;
     }
   }
   b[m] = acc[0];
