@@ -127,9 +127,10 @@ size_t rve_bytes(long long ns, int nphase) {
          align256(8 * 72 * (size_t)nphase) + align256(4 * 6 * ns) + align256(sizeof(PhaseMat) * (size_t)nphase);
 }
 
-size_t job_bytes(int nx, int ny, int nz) {
+size_t job_bytes(int nx, int ny, int nz, int nphase) {
   const long long ns = (long long)nx * ny * nz, n3 = 3 * ns;
   return 3 * align256(8 * n3) + 6 * align256(4 * n3) + align256(8 * max_halo_doubles(nx, ny, nz)) +
+         align256(8 * 6 * (size_t)nphase) +
          align256(8 * kJobSlots * kMaxParts) + align256(sizeof(GridBarrier)) + align256(sizeof(PcgState)) + align256(4) +
          align256(sizeof(JobResult));
 }
@@ -209,6 +210,7 @@ void fill_job(JobDev& J, const RveDev& R, char*& p, const double strain[6], int 
   d.h0 = carve<float>(p, n3);
   d.h1 = carve<float>(p, n3);
   d.Ah = carve<float>(p, n3);
+  d.sig = carve<double>(p, 6 * (size_t)R.nphase);
   J.halo_cap = max_halo_doubles(R.nx, R.ny, R.nz);
   double* halo = carve<double>(p, (size_t)J.halo_cap);
   d.hx = halo;  // split per k in set_parts
@@ -510,7 +512,7 @@ int32_t e3d_batch_create(e3d_batch_t** out, const e3d_rve_t* rves, int32_t n, co
   for (int r = 0; r < n; ++r) {
     const e3d_rve_t& R = rves[r];
     total += rve_bytes((long long)R.nx * R.ny * R.nz, R.ngrains + 1);
-    total += cases.size() * job_bytes(R.nx, R.ny, R.nz);
+    total += cases.size() * job_bytes(R.nx, R.ny, R.nz, R.ngrains + 1);
   }
   if (o->hbm_budget > 0 && (int64_t)total > o->hbm_budget) return fail(E3D_ERR_OOM);
   if (cudaMalloc(&b->pool, total) != cudaSuccess) {
@@ -752,7 +754,7 @@ int32_t e3d_serve_submit(e3d_server_t* s, const e3d_rve_t* rve, const double str
   j->rve.pix = j->pix.data();
   j->rve.rodrigues = j->rod.data();
   std::memcpy(j->strain, strain, sizeof j->strain);
-  j->bytes = rve_bytes(ns, rve->ngrains + 1) + job_bytes(rve->nx, rve->ny, rve->nz);
+  j->bytes = rve_bytes(ns, rve->ngrains + 1) + job_bytes(rve->nx, rve->ny, rve->nz, rve->ngrains + 1);
   if (s->opts.hbm_budget > 0 && (int64_t)j->bytes > s->opts.hbm_budget) {
     delete j;
     return E3D_ERR_OOM;  // could never be admitted

@@ -46,6 +46,7 @@ struct JobDesc {
   int nphase_total;
   const float* minv32;  // [6][ns] of the RVE
   // per job
+  double* sig;  // [nphase_total][6]: each phase's stress under the job's macro strain (set-up scratch)
   double* u;
   double* g;
   double* b;
@@ -197,38 +198,6 @@ static __device__ __noinline__ double job_c_elem(const JobDesc& J, int x, int y,
   return 0.5 * e;
 }
 
-// Boundary nodes (x, y or z on a face of the box), each once: the two x faces
-// whole, then the y faces at interior x, then the z faces at interior x and y.
-// Consecutive indices are consecutive x where the set allows, so a warp's
-// lanes share the work of job_b_node instead of idling beside one boundary lane.
-__device__ __forceinline__ long long boundary_node_count(const GridDims& G) {
-  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1, fz = G.nz > 1 ? 2 : 1;
-  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
-  return fx * G.ny * G.nz + ix * fy * G.nz + ix * iy * fz;
-}
-
-__device__ __forceinline__ void boundary_node(const GridDims& G, long long t, int& x, int& y, int& z) {
-  const long long fx = G.nx > 1 ? 2 : 1, fy = G.ny > 1 ? 2 : 1;
-  const long long ix = G.nx > 2 ? G.nx - 2 : 0, iy = G.ny > 2 ? G.ny - 2 : 0;
-  const long long na = fx * G.ny * G.nz, nb = ix * fy * G.nz;
-  if (t < na) {
-    const long long r = t / fx;
-    x = (t % fx) == 0 ? 0 : G.nx - 1;
-    y = (int)(r % G.ny);
-    z = (int)(r / G.ny);
-  } else if (t < na + nb) {
-    const long long s = t - na, r = s / ix;
-    x = 1 + (int)(s % ix);
-    y = (r % fy) == 0 ? 0 : G.ny - 1;
-    z = (int)(r / fy);
-  } else {
-    const long long s = t - na - nb, r = s / ix;
-    x = 1 + (int)(s % ix);
-    y = 1 + (int)(r % iy);
-    z = (r / iy) == 0 ? 0 : G.nz - 1;
-  }
-}
-
 // Elements with a corner across a high face (i = nx-1, j = ny-1 or k = nz-1),
 // each once, as femat_c_kernel enumerates them.
 __device__ __forceinline__ long long boundary_element_count(const GridDims& G) {
@@ -252,6 +221,48 @@ __device__ __forceinline__ void boundary_element(const GridDims& G, long long t,
     i = (int)(s % (G.nx - 1));
     j = (int)(s / (G.nx - 1));
   }
+}
+
+// Stress of every phase under the job's macro strain, sigma = cmod . eps
+// (engineering shear), for the start gradient below.
+static __device__ __noinline__ void job_phase_stress(const JobDesc& J, int part) {
+  const double e[6] = {J.J.E[0][0], J.J.E[1][1], J.J.E[2][2], 2.0 * J.J.E[0][2], 2.0 * J.J.E[1][2], 2.0 * J.J.E[0][1]};
+  const int np = J.nphase_total;
+  for (long long ph = (long long)part * NT + threadIdx.x; ph < np; ph += (long long)J.nparts * NT) {
+    for (int r = 0; r < 6; ++r) {
+      double v = 0.0;
+      for (int c = 0; c < 6; ++c) v += J.cmod[ph + (long long)np * (r + 6 * c)] * e[c];
+      J.sig[E3D_IDX(6 * ph + r, 6LL * np)] = v;
+    }
+  }
+}
+
+// Start gradient g0 = K u_affine + b at node (x, y, z), in closed form.  The
+// affine field E.x, continued across the periodic jumps, is E.x_e on every
+// element e, whose first-order Walsh-Hadamard components are 4 eps and whose
+// modal force is then the constant mode's sigma_e / 4 alone; back at the
+// corners that is sigma_e . s / 4, s = +-1 per axis (+ on the element's high
+// side).  Summed over the node's eight elements this is K u_affine + b exactly
+// -- the interface forces of the piecewise-constant stress -- at about a
+// quarter of a stencil pass's FP64 work and without the cancellation between
+// K u_affine and b at the box faces.
+static __device__ __forceinline__ void job_start_force(const JobDesc& J, int x, int y, int z, double (&g)[3]) {
+  const GridDims& G = J.G;
+  g[0] = g[1] = g[2] = 0.0;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int ox = a & 1, oy = (a >> 1) & 1, oz = (a >> 2) & 1;
+    const int ex = wrapi(x - ox, G.nx), ey = wrapi(y - oy, G.ny), ez = wrapi(z - oz, G.nz);
+    const int ph = J.pix[E3D_IDX((long long)ex + (long long)G.nx * ey + (long long)G.nx * G.ny * ez, G.ns)];
+    const double* sg = J.sig + E3D_IDX(6LL * ph, 6LL * J.nphase_total);
+    const double sx = ox ? 1.0 : -1.0, sy = oy ? 1.0 : -1.0, sz = oz ? 1.0 : -1.0;
+    g[0] += sx * sg[0] + sy * sg[5] + sz * sg[3];
+    g[1] += sx * sg[5] + sy * sg[1] + sz * sg[4];
+    g[2] += sx * sg[3] + sy * sg[4] + sz * sg[2];
+  }
+  g[0] *= 0.25;
+  g[1] *= 0.25;
+  g[2] *= 0.25;
 }
 
 template <typename T>
@@ -329,6 +340,36 @@ static __device__ __noinline__ bool job_true_residual(const JobDesc& J, int part
       const double gd = v[c] + bi;
       gg += gd * gd;
       J.g[i] = gd;
+      gv[c] = (float)gd;
+      J.g32[i] = gv[c];
+    }
+    float zv[3];
+    precond3<float>(J.minv32, m, ns, gv, zv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) J.z32[m + c * ns] = zv[c];
+    zg += (double)(zv[0] * gv[0] + zv[1] * gv[1] + zv[2] * gv[2]);
+  });
+  job_put(J, SL_ZG, part, zg, red);
+  job_put(J, SL_U, part, eu, red);
+  job_put(J, SL_GG, part, gg, red);
+  return job_barrier(J.bar, J.nparts, err, to);
+}
+
+// The set-up's counterpart of job_true_residual: g already holds the whole
+// start gradient K u + b (job_start_force), so g32, z32 and the partials of
+// z.g, g.g and the energy terms u.(Ku)/2 + b.u = u.(g + b)/2 follow directly.
+static __device__ __noinline__ bool job_start_residual(const JobDesc& J, int part, double* red, int* err,
+                                                      unsigned long long to) {
+  const long long ns = J.G.ns;
+  double zg = 0.0, eu = 0.0, gg = 0.0;
+  for_part_nodes(J, part, [&](long long m, int, int, int, int, int, int, int, int, int) {
+    float gv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long i = m + c * ns;
+      const double gd = J.g[i];
+      eu += 0.5 * J.u[i] * (gd + J.b[i]);
+      gg += gd * gd;
       gv[c] = (float)gd;
       J.g32[i] = gv[c];
     }
@@ -465,15 +506,23 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       double cpart = 0.0;
       const double exx = J.J.E[0][0], eyy = J.J.E[1][1], ezz = J.J.E[2][2];
       const double exy = J.J.E[0][1], exz = J.J.E[0][2], eyz = J.J.E[1][2];
-      for_part_nodes(J, part, [&](long long m, int x, int y, int z, int, int, int, int, int, int) {
-        if (!(x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1))
-          J.b[m] = J.b[m + ns] = J.b[m + 2 * ns] = 0.0;  // boundary nodes: below
-        const double xd = x, yd = y, zd = z;
-        J.u[m] = xd * exx + yd * exy + zd * exz;
-        J.u[m + ns] = xd * exy + yd * eyy + zd * eyz;
-        J.u[m + 2 * ns] = xd * exz + yd * eyz + zd * ezz;
-        J.du[m] = J.du[m + ns] = J.du[m + 2 * ns] = 0.0f;
-      });
+      job_phase_stress(J, part);
+      ok = job_barrier(J.bar, J.nparts, E.err, to);
+      if (ok)
+        for_part_nodes(J, part, [&](long long m, int x, int y, int z, int, int, int, int, int, int) {
+          if (!(x == 0 || x == G.nx - 1 || y == 0 || y == G.ny - 1 || z == 0 || z == G.nz - 1))
+            J.b[m] = J.b[m + ns] = J.b[m + 2 * ns] = 0.0;  // boundary nodes: below
+          const double xd = x, yd = y, zd = z;
+          J.u[m] = xd * exx + yd * exy + zd * exz;
+          J.u[m + ns] = xd * exy + yd * eyy + zd * eyz;
+          J.u[m + 2 * ns] = xd * exz + yd * eyz + zd * ezz;
+          J.du[m] = J.du[m + ns] = J.du[m + 2 * ns] = 0.0f;
+          double g0[3];
+          job_start_force(J, x, y, z, g0);
+          J.g[m] = g0[0];
+          J.g[m + ns] = g0[1];
+          J.g[m + 2 * ns] = g0[2];
+        });
       // b at the boundary nodes and C over the boundary elements, both listed
       // compactly and shared by all threads of all parts
       const long long stride = (long long)J.nparts * NT, first = (long long)part * NT + threadIdx.x;
@@ -495,9 +544,8 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
         cpart += job_c_elem(J, i, j, k);
       }
       job_put(J, SL_C, part, cpart, red);
-      ok = job_barrier(J.bar, J.nparts, E.err, to);
-      if (ok) ok = job_fp64_apply_u(J, part, sm64, E.err, to);
-      if (ok) ok = job_true_residual(J, part, true, red, E.err, to);
+      if (ok) ok = job_barrier(J.bar, J.nparts, E.err, to);
+      if (ok) ok = job_start_residual(J, part, red, E.err, to);
       if (ok) {
         const double C = job_reduce(J, SL_C, red);
         const double U0 = C + job_reduce(J, SL_U, red);
