@@ -304,3 +304,34 @@ def test_laminate_matches_the_closed_form(axis):
             assert _rel(r["strav"], sig) < 1e-12
         else:
             assert 0 <= r["utot"] - w * p.ns <= 1e-8 * w * p.ns
+
+
+def test_start_gradient_is_the_interface_force_of_the_affine_stress():
+    """K u_affine + b (the gradient at the reference's affine start guess,
+    src/elas3dxtal_pcg.f90:423-438 and :1332-1340) equals, node by node, the
+    sum over the node's eight elements of sigma_e . s / 4 with sigma_e =
+    cmod_e . eps and s = +-1 per axis (+ on the element's high side) -- the
+    closed form the job engine's set-up uses instead of a stencil pass."""
+    p, pix, rod, s = _rand_problem(7, 6, 5, 4, seed=77, strain=[1e-3, -4e-4, 2e-4, 3e-4, -1e-4, 5e-4])
+    o = O.Oracle(p, pix, rod).femat()
+    g, U = o.energy(o.affine_u())
+    cm = o.cmod_array()
+    eps = s * np.array([1, 1, 1, 2, 2, 2])
+    sig = cm @ eps  # [phase, 6]
+    nx, ny, nz = p.nx, p.ny, p.nz
+    ph = (pix - 1).reshape(nz, ny, nx)
+    g0 = np.zeros((3, nz, ny, nx))
+    for a in range(8):
+        ox, oy, oz = a & 1, (a >> 1) & 1, (a >> 2) & 1
+        # element with lower corner (x-ox, y-oy, z-oz), periodic
+        pe = np.roll(ph, shift=(oz, oy, ox), axis=(0, 1, 2))
+        sg = sig[pe]  # [z, y, x, 6]
+        sx, sy, sz = (1.0 if ox else -1.0), (1.0 if oy else -1.0), (1.0 if oz else -1.0)
+        g0[0] += sx * sg[..., 0] + sy * sg[..., 5] + sz * sg[..., 3]
+        g0[1] += sx * sg[..., 5] + sy * sg[..., 1] + sz * sg[..., 4]
+        g0[2] += sx * sg[..., 3] + sy * sg[..., 4] + sz * sg[..., 2]
+    g0 = 0.25 * g0.reshape(3, -1).ravel()
+    assert np.max(np.abs(g0 - g)) <= 1e-12 * np.max(np.abs(g))
+    # and the start energy C + sum(u.Ku/2 + b.u) = C + sum(u.(g + b))/2
+    u = o.affine_u()
+    assert abs(o.C + 0.5 * u @ (g0 + o.b) - U) <= 1e-12 * abs(U)
