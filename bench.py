@@ -622,7 +622,7 @@ def form_serve(args) -> dict:
     budget = int(150e9)
     crit = e3d.CRIT_PRECOND_REL if args.criterion == "precond" else e3d.CRIT_REF
     srv = e3d.Server(max_active=args.slots, round_iters=args.round_iters, max_iter=20000, hbm_budget=budget,
-                     refine_every=args.refine_every,
+                     refine_every=args.refine_every, round_balance=bool(args.round_balance),
                      criterion=crit)
     clocks = ClockSampler(0).start()
     t0 = time.perf_counter()
@@ -673,6 +673,7 @@ def form_serve(args) -> dict:
             "continuous_batching": {"arrived_while_busy": busy_arrivals, "max_pending": max_pending,
                                     "slots": args.slots, "rounds": rounds},
             "peak_hbm_bytes": peak, "hbm_budget": budget, "round_iters": args.round_iters,
+            "round_balance": bool(args.round_balance),
             "criterion": args.criterion, "clocks": clk,
             "work": {"node_iterations": node_iters, "dof_iters_per_s": 3.0 * node_iters / total,
                      "iterations": {"min": int(min(r["iterations"] for r in res)),
@@ -720,6 +721,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=32, help="serve: concurrent solves")
     ap.add_argument("--round-iters", type=int, default=50, help="serve: iterations per solve per round")
+    ap.add_argument("--round-balance", type=int, default=1,
+                    help="serve: 1 = smaller solves run up to 8x round-iters per round (0 = fixed rounds)")
     ap.add_argument("--serve-max-edge", type=int, default=256)
     ap.add_argument("--sample", type=int, default=32, help="batch/serve: sequential FP64 reference sample")
     ap.add_argument("--criterion", choices=["ref", "precond"], default="ref",

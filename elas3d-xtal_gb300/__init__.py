@@ -673,7 +673,7 @@ class ServeOptsC(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_iter", C.c_int32), ("refine_every", C.c_int32),
                 ("criterion", C.c_int32), ("divergence_reset", C.c_int32), ("tol", C.c_float),
                 ("max_active", C.c_int32), ("round_iters", C.c_int32), ("parts", C.c_int32),
-                ("pad", C.c_int32), ("e1", C.c_double), ("nu1", C.c_double), ("hbm_budget", C.c_int64)]
+                ("round_balance", C.c_int32), ("e1", C.c_double), ("nu1", C.c_double), ("hbm_budget", C.c_int64)]
 
 
 BATCH_SYMBOLS = ("e3d_batch_opts_defaults", "e3d_batch_create", "e3d_batch_solve", "e3d_batch_results",
@@ -779,12 +779,13 @@ class Server:
     """Continuous-batching solve server (admission by slots and HBM budget)."""
 
     def __init__(self, *, max_active=64, round_iters=50, max_iter=10000, refine_every=50, tol=1e-8,
-                 criterion=CRIT_REF, parts=0, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
+                 criterion=CRIT_REF, parts=0, round_balance=True, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
         self.L = _bind_batch(load_library())
         o = ServeOptsC()
         self.L.e3d_serve_opts_defaults(C.byref(o))
         o.device, o.max_active, o.round_iters, o.max_iter = device, max_active, round_iters, max_iter
         o.refine_every, o.tol, o.criterion, o.parts = refine_every, tol, criterion, parts
+        o.round_balance = 1 if round_balance else 0
         o.e1, o.nu1, o.hbm_budget = e1, nu1, hbm_budget
         self._h = C.c_void_p()
         _check(self.L.e3d_serve_create(C.byref(self._h), C.byref(o)), "e3d_serve_create")

@@ -658,6 +658,7 @@ int32_t e3d_batch_parts(e3d_batch_t* b, int32_t* parts, int32_t capacity) {
 // ============================================================== server
 struct ServeJob {
   int64_t id = 0;
+  int parts = 1;  // blocks per solve, fixed at admission
   e3d_rve_t rve{};
   std::vector<int32_t> pix;
   std::vector<double> rod;
@@ -681,8 +682,26 @@ struct e3d_server {
   std::vector<ServeJob*> active;
   std::map<int64_t, ServeJob*> finished;
   int64_t bytes_now = 0, bytes_peak = 0;
+  int blocks_now = 0;  // parts of the active solves: kept within the engine's resident blocks
   std::vector<int32_t> scratch;
 };
+
+// Nodes per block the serving loop aims at when it splits a solve into parts.
+#ifndef E3D_SERVE_BLOCK_NODES
+#define E3D_SERVE_BLOCK_NODES 131072
+#endif
+
+// Iterations per round of one solve: round_iters, or with round balancing
+// round_iters x (target nodes per block / this solve's nodes per block), within
+// [1, 8] x round_iters, so that a small solve's block is not left idle while
+// the large solves' blocks finish the round.  A function of the solve alone:
+// its results do not depend on what else is on the device.
+int serve_round_iters(const e3d_serve_opts_t& o, long long ns, int k) {
+  if (!o.round_balance) return o.round_iters;
+  const double per_block = (double)ns / k;
+  const double f = std::min(8.0, std::max(1.0, (double)E3D_SERVE_BLOCK_NODES / per_block));
+  return (int)std::min<double>(2.0e9, std::floor(o.round_iters * f));
+}
 
 extern "C" {
 
@@ -697,6 +716,7 @@ void e3d_serve_opts_defaults(e3d_serve_opts_t* o) {
   o->max_active = 64;
   o->round_iters = 50;
   o->parts = 0;
+  o->round_balance = 1;
   o->hbm_budget = 0;
 }
 
@@ -769,10 +789,18 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
   E3D_TRACE("e3d_serve_step");
   if (!s) return E3D_ERR_INPUT;
   cudaSetDevice(s->device);
-  // admit in arrival order while slots and budget allow
+  // admit in arrival order while slots, the HBM budget and the engine's
+  // resident blocks allow: every part of every active solve then runs at once,
+  // so no part waits at a job barrier for a sibling that has no block yet
   while (!s->queue.empty() && (int)s->active.size() < s->opts.max_active) {
     ServeJob* j = s->queue.front();
     if (s->opts.hbm_budget > 0 && s->bytes_now + (int64_t)j->bytes > s->opts.hbm_budget) break;
+    {
+      const long long ns_j = (long long)j->rve.nx * j->rve.ny * j->rve.nz;
+      const int kk = s->opts.parts > 0 ? std::min(s->opts.parts, kMaxParts) : default_parts(ns_j);
+      j->parts = std::min(kk, s->eng.grid);
+      if (!s->active.empty() && s->blocks_now + j->parts > s->eng.grid) break;
+    }
     cudaError_t e = cudaMallocAsync(&j->mem, j->bytes, s->stream);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -797,9 +825,10 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
     }
     fill_job(j->J, j->R, p, j->strain, s->opts.max_iter, s->opts.refine_every, s->opts.criterion,
              s->opts.divergence_reset, s->opts.tol);
-    const int k = s->opts.parts > 0 ? std::min(s->opts.parts, kMaxParts) : default_parts(ns);
-    set_parts(j->J, j->R, std::min(k, s->eng.grid));
+    set_parts(j->J, j->R, j->parts);
+    j->J.d.it_round = serve_round_iters(s->opts, ns, j->parts);
     BCUDA(cudaMemsetAsync(j->J.d.stage, 0, 4, s->stream));
+    s->blocks_now += j->parts;
     s->active.push_back(j);
   }
   if (!s->active.empty()) {
@@ -848,6 +877,7 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
       cudaFreeAsync(j->mem, s->stream);
       j->mem = nullptr;
       s->bytes_now -= (int64_t)j->bytes;
+      s->blocks_now -= j->parts;
       j->pix.clear();
       j->pix.shrink_to_fit();
       s->finished[j->id] = j;
@@ -902,6 +932,7 @@ int32_t e3d_serve_cancel(e3d_server_t* s, int64_t id) {
       BCUDA(cudaFreeAsync(j->mem, s->stream));
       j->mem = nullptr;
       s->bytes_now -= (int64_t)j->bytes;
+      s->blocks_now -= j->parts;
       s->active.erase(it);
       finish(j, stage == JOB_NEW ? 0 : st.it);
       return E3D_OK;

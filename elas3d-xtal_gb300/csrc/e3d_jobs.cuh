@@ -65,6 +65,7 @@ struct JobDesc {
   int* stage;
   JobResult* out;
   int nparts;
+  int it_round;  // iterations per engine launch for this solve (0: the launch's it_limit)
   int max_iter;
   int refine_every;
   int criterion;
@@ -584,7 +585,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
     __syncthreads();
     // ---------------- FP32 inner iterations with FP64 residual replacement
     const int R = J.refine_every > 0 ? J.refine_every : 50;
-    const int it_end = min(s.it + E.it_limit, s.max_iter);
+    const int it_end = min(s.it + (J.it_round > 0 ? J.it_round : E.it_limit), s.max_iter);
     while (ok && s.status == PCG_RUNNING && s.it < it_end) {
       const int cur = s.cur;
       const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, sm32,

@@ -117,7 +117,7 @@ def workload(check):
         check(f"batch_parts{parts}")
     rng = np.random.default_rng(7)
     reqs = [(W.rve(n, 5, 200 + n, A=1.5), rng.normal(size=6) * 1e-3) for n in (14, 10, 18)]
-    with e3d.Server(round_iters=5, max_active=2) as srv:
+    with e3d.Server(round_iters=5, max_active=2, round_balance=False) as srv:
         ids = [srv.submit(*r) for r in reqs]
         srv.step()
         srv.cancel(ids[2])  # queued

@@ -42,11 +42,11 @@ def _drain(srv, ids, rounds=100000):
 def test_serve_results_match_oracle_and_mix():
     reqs = _requests()
     # alone: request 1 in a fresh server
-    with e3d.Server(round_iters=10) as srv:
+    with e3d.Server(round_iters=10, round_balance=False) as srv:
         rid = srv.submit(*reqs[1])
         alone = _drain(srv, [rid])[0]
     # mixed: staggered arrivals while others are on the device
-    with e3d.Server(round_iters=10) as srv:
+    with e3d.Server(round_iters=10, round_balance=False) as srv:
         ids = [srv.submit(*reqs[0]), srv.submit(*reqs[1])]
         srv.step()
         srv.step()
@@ -80,7 +80,7 @@ def test_serve_hbm_budget_bounds_admission():
 
 def test_serve_cancel_queued_and_active_requests():
     reqs = _requests()
-    with e3d.Server(round_iters=5, max_active=2) as srv:
+    with e3d.Server(round_iters=5, max_active=2, round_balance=False) as srv:
         ids = [srv.submit(*r) for r in reqs[:4]]
         srv.step()  # requests 0 and 1 active, 2 and 3 queued
         srv.cancel(ids[1])  # active
@@ -112,3 +112,24 @@ def test_serve_refuses_bad_phase_ids_at_submission():
         rid = srv.submit(rve, strain)  # the server is unaffected
         out = _drain(srv, [rid])
     assert out[0]["status"] == e3d.EXIT_CONVERGED
+
+
+def test_serve_round_balance_changes_scheduling_only():
+    """With round balancing a small solve runs more iterations per round than
+    a large one; results are a function of the request alone, so they are
+    bitwise those of fixed rounds, in fewer rounds."""
+    reqs = _requests()
+    out, rounds = {}, {}
+    for bal in (False, True):
+        with e3d.Server(round_iters=8, round_balance=bal) as srv:
+            ids = [srv.submit(*r) for r in reqs]
+            n = 0
+            while srv.step() > 0:
+                n += 1
+            out[bal] = [srv.result(i) for i in ids]
+            rounds[bal] = n
+    for a, b in zip(out[False], out[True]):
+        assert a["status"] == b["status"] == e3d.EXIT_CONVERGED
+        assert a["iterations"] == b["iterations"] and a["utot"] == b["utot"]
+        assert np.array_equal(a["strav"], b["strav"])
+    assert rounds[True] < rounds[False]
