@@ -68,7 +68,7 @@ def test_serve_hbm_budget_bounds_admission():
     with e3d.Server(round_iters=20) as probe:
         probe.submit(*reqs[4])
         probe.step()
-        one, _ = probe.memory()
+        _, one = probe.memory()  # peak: the request may already be done after one round
     budget = int(one * 1.5)  # room for the largest request alone
     with e3d.Server(round_iters=20, hbm_budget=budget) as srv:
         ids = [srv.submit(*r) for r in reqs]
