@@ -721,7 +721,7 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=32, help="serve: concurrent solves")
     ap.add_argument("--round-iters", type=int, default=50, help="serve: iterations per solve per round")
-    ap.add_argument("--round-balance", type=int, default=1,
+    ap.add_argument("--round-balance", type=int, default=0,
                     help="serve: 1 = smaller solves run up to 8x round-iters per round (0 = fixed rounds)")
     ap.add_argument("--serve-max-edge", type=int, default=256)
     ap.add_argument("--sample", type=int, default=32, help="batch/serve: sequential FP64 reference sample")

@@ -779,7 +779,7 @@ class Server:
     """Continuous-batching solve server (admission by slots and HBM budget)."""
 
     def __init__(self, *, max_active=64, round_iters=50, max_iter=10000, refine_every=50, tol=1e-8,
-                 criterion=CRIT_REF, parts=0, round_balance=True, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
+                 criterion=CRIT_REF, parts=0, round_balance=False, e1=0.0, nu1=0.0, hbm_budget=0, device=0):
         self.L = _bind_batch(load_library())
         o = ServeOptsC()
         self.L.e3d_serve_opts_defaults(C.byref(o))

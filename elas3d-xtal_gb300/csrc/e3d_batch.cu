@@ -682,7 +682,6 @@ struct e3d_server {
   std::vector<ServeJob*> active;
   std::map<int64_t, ServeJob*> finished;
   int64_t bytes_now = 0, bytes_peak = 0;
-  int blocks_now = 0;  // parts of the active solves: kept within the engine's resident blocks
   std::vector<int32_t> scratch;
 };
 
@@ -716,7 +715,7 @@ void e3d_serve_opts_defaults(e3d_serve_opts_t* o) {
   o->max_active = 64;
   o->round_iters = 50;
   o->parts = 0;
-  o->round_balance = 1;
+  o->round_balance = 0;
   o->hbm_budget = 0;
 }
 
@@ -789,9 +788,7 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
   E3D_TRACE("e3d_serve_step");
   if (!s) return E3D_ERR_INPUT;
   cudaSetDevice(s->device);
-  // admit in arrival order while slots, the HBM budget and the engine's
-  // resident blocks allow: every part of every active solve then runs at once,
-  // so no part waits at a job barrier for a sibling that has no block yet
+  // admit in arrival order while slots and budget allow
   while (!s->queue.empty() && (int)s->active.size() < s->opts.max_active) {
     ServeJob* j = s->queue.front();
     if (s->opts.hbm_budget > 0 && s->bytes_now + (int64_t)j->bytes > s->opts.hbm_budget) break;
@@ -799,7 +796,6 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
       const long long ns_j = (long long)j->rve.nx * j->rve.ny * j->rve.nz;
       const int kk = s->opts.parts > 0 ? std::min(s->opts.parts, kMaxParts) : default_parts(ns_j);
       j->parts = std::min(kk, s->eng.grid);
-      if (!s->active.empty() && s->blocks_now + j->parts > s->eng.grid) break;
     }
     cudaError_t e = cudaMallocAsync(&j->mem, j->bytes, s->stream);
     if (e != cudaSuccess) {
@@ -828,7 +824,6 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
     set_parts(j->J, j->R, j->parts);
     j->J.d.it_round = serve_round_iters(s->opts, ns, j->parts);
     BCUDA(cudaMemsetAsync(j->J.d.stage, 0, 4, s->stream));
-    s->blocks_now += j->parts;
     s->active.push_back(j);
   }
   if (!s->active.empty()) {
@@ -877,7 +872,6 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
       cudaFreeAsync(j->mem, s->stream);
       j->mem = nullptr;
       s->bytes_now -= (int64_t)j->bytes;
-      s->blocks_now -= j->parts;
       j->pix.clear();
       j->pix.shrink_to_fit();
       s->finished[j->id] = j;
@@ -932,7 +926,6 @@ int32_t e3d_serve_cancel(e3d_server_t* s, int64_t id) {
       BCUDA(cudaFreeAsync(j->mem, s->stream));
       j->mem = nullptr;
       s->bytes_now -= (int64_t)j->bytes;
-      s->blocks_now -= j->parts;
       s->active.erase(it);
       finish(j, stage == JOB_NEW ? 0 : st.it);
       return E3D_OK;

@@ -95,8 +95,8 @@ typedef struct e3d_serve_opts {
   int32_t round_iters;      /* PCG iterations per solve per engine round          */
   int32_t parts;            /* blocks per solve (<= 64): 0 = by size              */
   int32_t round_balance;    /* 1: a solve with fewer nodes per block runs up to
-                               8x round_iters per round, so all blocks of a round
-                               finish together; 0: round_iters for every solve   */
+                               8x round_iters per round (same results, fewer
+                               rounds); 0 (default): round_iters for every solve */
   double e1, nu1;
   int64_t hbm_budget;       /* bytes of device memory the server may hold        */
 } e3d_serve_opts_t;
