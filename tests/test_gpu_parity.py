@@ -1,7 +1,7 @@
 """Parity of the CUDA library (called through the C ABI) against the CPU
 oracle on the same seeded inputs.
 
-Tolerances (spec contract for the plain FP64 path):
+Tolerances of the plain FP64 path:
   K.u                      1e-12 relative (norm-wise)
   dk, cmod, b, C, Minv     1e-12 relative (max-norm over the array)
   converged energy, <sigma> 1e-9 relative, iteration count within +-2
