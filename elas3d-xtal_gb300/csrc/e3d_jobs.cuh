@@ -395,6 +395,9 @@ static __device__ __noinline__ bool job_start_residual(const JobDesc& J, int par
 #ifndef E3D_ENGINE_TAB_ASYNC
 #define E3D_ENGINE_TAB_ASYNC 0  // stiffness rows staged one plane ahead (E3D_F32_TAB_ASYNC; slower there)
 #endif
+#ifndef E3D_ENGINE_POLD_SMEM
+#define E3D_ENGINE_POLD_SMEM E3D_F32_POLD_SMEM  // lower node plane re-read from shared memory (1) or kept in registers (0)
+#endif
 static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
                                                      ApplySmem<float>& sm, float4* tab) {
   __shared__ ApplyArgs<float> sA;
@@ -413,7 +416,7 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
   const long long nt = J.G.ntiles;
   const int np = J.nparts;
   for (long long t = part; t < nt; t += np) {
-    apply_tile<float, true, E3D_F32_POLD_SMEM != 0, false, E3D_ENGINE_TAB_ASYNC != 0>(sA, t, sm, hAh, tab);
+    apply_tile<float, true, E3D_ENGINE_POLD_SMEM != 0, false, E3D_ENGINE_TAB_ASYNC != 0>(sA, t, sm, hAh, tab);
     __syncthreads();
   }
   return hAh;
