@@ -398,8 +398,11 @@ static __device__ __noinline__ bool job_start_residual(const JobDesc& J, int par
 #ifndef E3D_ENGINE_POLD_SMEM
 #define E3D_ENGINE_POLD_SMEM E3D_F32_POLD_SMEM  // lower node plane re-read from shared memory (1) or kept in registers (0)
 #endif
+#ifndef E3D_ENGINE_DEFER_U
+#define E3D_ENGINE_DEFER_U 0  // du -= lam h of iteration k applied in phase A of k+1 (as E3D_F32_DEFER_U)
+#endif
 static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, int part, float gamma, int reset, int cur,
-                                                     ApplySmem<float>& sm, float4* tab) {
+                                                     float lam_prev, ApplySmem<float>& sm, float4* tab) {
   __shared__ ApplyArgs<float> sA;
   if (threadIdx.x == 0) {
     ApplyArgs<float> A = job_apply_args<float>(J);
@@ -409,6 +412,8 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
     A.y = J.Ah;
     A.gamma = gamma;
     A.reset = reset;
+    A.du = J.du;
+    A.lam_prev = lam_prev;
     sA = A;
   }
   __syncthreads();
@@ -416,7 +421,8 @@ static __device__ E3D_ENGINE_SWEEP_ATTR double job_fp32_apply(const JobDesc& J, 
   const long long nt = J.G.ntiles;
   const int np = J.nparts;
   for (long long t = part; t < nt; t += np) {
-    apply_tile<float, true, E3D_ENGINE_POLD_SMEM != 0, false, E3D_ENGINE_TAB_ASYNC != 0>(sA, t, sm, hAh, tab);
+    apply_tile<float, true, E3D_ENGINE_POLD_SMEM != 0, E3D_ENGINE_DEFER_U != 0, E3D_ENGINE_TAB_ASYNC != 0>(sA, t, sm,
+                                                                                                         hAh, tab);
     __syncthreads();
   }
   return hAh;
@@ -435,12 +441,13 @@ constexpr int kEngineDynSmem = (E3D_ENGINE_TAB_ASYNC && kTabAsyncBytes > kEngine
 // du -= lam h, g -= lam Ah, z = Minv g: returns this part's z.g.
 static __device__ __noinline__ double job_fp32_update(const JobDesc& J, int part, float lam, int cur, float* stages) {
   if constexpr (E3D_ENGINE_PB_ASYNC > 0)
-    return pcg_update_tiles_async<float, E3D_ENGINE_PB_ASYNC, true>(
+    return pcg_update_tiles_async<float, E3D_ENGINE_PB_ASYNC, E3D_ENGINE_DEFER_U == 0>(
         J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah, reinterpret_cast<const float*>(J.hx),
         reinterpret_cast<const float*>(J.hy), reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32,
         stages);
   else
-    return pcg_update_tiles<float>(J.G, part, J.nparts, lam, cur ? J.h0 : J.h1, J.Ah,
+    return pcg_update_tiles<float, E3D_PB_UNROLL_F32, E3D_ENGINE_DEFER_U == 0>(J.G, part, J.nparts, lam,
+                                                                                 cur ? J.h0 : J.h1, J.Ah,
                                    reinterpret_cast<const float*>(J.hx), reinterpret_cast<const float*>(J.hy),
                                    reinterpret_cast<const float*>(J.hd), J.minv32, J.du, J.g32, J.z32);
 }
@@ -589,10 +596,19 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
     // ---------------- FP32 inner iterations with FP64 residual replacement
     const int R = J.refine_every > 0 ? J.refine_every : 50;
     const int it_end = min(s.it + (J.it_round > 0 ? J.it_round : E.it_limit), s.max_iter);
+    // E3D_ENGINE_DEFER_U: du -= lam_pending * h_pending is still owed; the next
+    // phase A applies it, or flush_pending before du is read or the job yields
+    float lam_pending = 0.f;
+    const float* h_pending = nullptr;
+    auto flush_pending = [&]() {
+      if (E3D_ENGINE_DEFER_U && lam_pending != 0.f) flush_u_tiles<float>(G, part, J.nparts, lam_pending, h_pending, J.du);
+      lam_pending = 0.f;
+    };
     while (ok && s.status == PCG_RUNNING && s.it < it_end) {
       const int cur = s.cur;
-      const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, sm32,
+      const double hAh_t = job_fp32_apply(J, part, (float)s.gamma, s.reset, cur, lam_pending, sm32,
                                           reinterpret_cast<float4*>(e3d_engine_dyn));
+      lam_pending = 0.f;  // applied by this phase A
       job_put(J, SL_A, part, hAh_t, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double hAh = job_reduce(J, SL_A, red);
@@ -609,6 +625,10 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       if (s.status != PCG_RUNNING) break;
       const float lam = (float)(s.gg / hAh);
       const double zg = job_fp32_update(J, part, lam, cur, pb_stages);
+      if (E3D_ENGINE_DEFER_U) {
+        lam_pending = lam;
+        h_pending = cur ? J.h0 : J.h1;  // the h_new of this iteration's phase A
+      }
       job_put(J, SL_B, part, zg, red);
       if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
       const double gg_new = job_reduce(J, SL_B, red);
@@ -646,6 +666,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
       // ends within about two decades, 1e-3 adds no replacement and 1e-2 adds one)
       if (s.status == PCG_CONVERGED || s.since_replace >= R || s.rel_res < kRefineDrop * s.rel_at_replace) {
         // FP64 residual replacement: u += du, g = K u + b, restart the FP32 recurrence
+        flush_pending();
         job_fold(J, part);
         if (!(ok = job_barrier(J.bar, J.nparts, E.err, to))) break;
         if (!(ok = job_fp64_apply_u(J, part, sm64, E.err, to))) break;
@@ -672,6 +693,7 @@ static __global__ void __launch_bounds__(NT, E3D_ENGINE_BLOCKS_PER_SM) job_engin
         __syncthreads();
       }
     }
+    flush_pending();  // the part's own nodes, as phase A owns them: no barrier needed before the fold
     __syncthreads();
     if (lead) {
       if (!ok) s.status = PCG_TIMEOUT;
