@@ -118,3 +118,71 @@ def test_serve_laminate_requests_are_exact():
         ns = int(np.prod(rve["shape"]))
         assert abs(r["utot"] - w * ns) <= 1e-8 * w * ns
         assert _rel(r["strav"], sig_avg) < 1e-7
+
+
+@pytest.mark.parametrize("flag_m,precision", [(1, e3d.PREC_FP64), (0, e3d.PREC_FP64), (1, e3d.PREC_MIXED)])
+def test_laminate_with_isotropic_inclusion_layers(flag_m, precision):
+    """Layers of the isotropic inclusion phase (E1 = 380 GPa, nu1 = 0.27)
+    between rotated cubic grains (flag_m = 1) or isotropic matrix phases
+    (flag_m = 0): the phase tables of both material modes against the closed
+    form, on a 64 x 40 x 150 laminate."""
+    rng = np.random.default_rng(120 + flag_m)
+    shape, axis, ng = (64, 40, 150), 2, 6
+    layers = rng.integers(1, ng + 2, size=shape[axis])
+    layers[:2] = [ng + 1, 1]
+    pix = AN.laminate_pix(shape, layers, axis)
+    rod = rng.normal(size=3 * ng)
+    kw = dict(flag_m=flag_m, c11=W.C11, c12=W.C12, c44=W.c44_from_zener(2.5), e1=380e9, nu1=0.27)
+    tol = 1e-10 if precision == e3d.PREC_FP64 else 1e-8
+    p = e3d.Problem(*shape, ng + 1, strain=STRAIN, tol=tol, criterion=e3d.CRIT_PRECOND_REL, precision=precision,
+                    refine_every=50, **kw)
+    with e3d.Elas3D(p) as g:
+        g.upload(pix, rod)
+        res = g.run()
+    # the phase tables depend on the constants and orientations only: a 2 x 2 x 2 oracle problem gives them
+    tiny = O.Problem(2, 2, 2, ng + 1, **kw)
+    cm = O.Oracle(tiny, np.ones(8, np.int32), rod).femat().cmod_array()
+    w, sig_avg, _ = AN.laminate_exact(cm, layers, AN.engineering(STRAIN), axis)
+    assert res["exit_reason"] == e3d.EXIT_CONVERGED
+    etol, stol = (1e-10, 1e-10) if precision == e3d.PREC_FP64 else (1e-8, 1e-7)
+    assert abs(res["utot"] - w * p.ns) <= etol * w * p.ns
+    assert _rel(res["strav"], sig_avg) < stol
+
+
+def test_plain_cg_laminate_is_exact():
+    """The identity-preconditioner variant (applications/sec3_1/cg) reaches the
+    same closed form."""
+    layers, pix, rod, c44, cm = _laminate(2, (40, 24, 60), 2.0)
+    p = e3d.Problem(40, 24, 60, len(rod) // 3 + 1, c11=W.C11, c12=W.C12, c44=c44, strain=STRAIN, tol=1e-10,
+                    criterion=e3d.CRIT_PRECOND_REL, preconditioner=e3d.PRECOND_NONE, max_iter=50000)
+    with e3d.Elas3D(p) as g:
+        g.upload(pix, rod)
+        res = g.run()
+    w, sig_avg, _ = AN.laminate_exact(cm, layers, AN.engineering(STRAIN), 2)
+    assert res["exit_reason"] == e3d.EXIT_CONVERGED
+    assert abs(res["utot"] - w * p.ns) <= 1e-10 * w * p.ns
+    assert _rel(res["strav"], sig_avg) < 1e-9
+
+
+def test_batch_laminates_with_inclusion_layers():
+    """Batched RVEs whose last phase is an isotropic inclusion (batch options
+    E1, nu1) in layers between the grains: C_eff against the closed form."""
+    rng = np.random.default_rng(130)
+    ng, e1, nu1 = 4, 380e9, 0.27
+    specs, rves = [(0, (30, 10, 12), 1.5), (2, (12, 10, 34), 4.0)], []
+    for i, (a, shape, A) in enumerate(specs):
+        layers = rng.integers(1, ng + 2, size=shape[a])
+        layers[:2] = [ng + 1, 1]
+        rod = rng.normal(size=3 * ng)
+        rve = dict(shape=shape, ngrains=ng, c11=W.C11, c12=W.C12, c44=W.c44_from_zener(A),
+                   pix=AN.laminate_pix(shape, layers, a), rodrigues=rod)
+        tiny = O.Problem(2, 2, 2, ng + 1, c11=W.C11, c12=W.C12, c44=rve["c44"], e1=e1, nu1=nu1)
+        cm = O.Oracle(tiny, np.ones(8, np.int32), rod).femat().cmod_array()
+        rves.append((rve, layers, cm, a))
+    with e3d.Batch([r[0] for r in rves], criterion=e3d.CRIT_PRECOND_REL, tol=1e-8, e1=e1, nu1=nu1) as b:
+        ceff, _ = b.solve()
+        res = b.results()
+    assert all(r["status"] == e3d.EXIT_CONVERGED for r in res)
+    for i, (_, layers, cm, a) in enumerate(rves):
+        exact = AN.laminate_ceff(cm, layers, a)
+        assert np.abs(ceff[i] - exact).max() <= 1e-7 * np.abs(exact).max(), i

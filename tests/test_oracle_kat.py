@@ -335,3 +335,28 @@ def test_start_gradient_is_the_interface_force_of_the_affine_stress():
     # and the start energy C + sum(u.Ku/2 + b.u) = C + sum(u.(g + b))/2
     u = o.affine_u()
     assert abs(o.C + 0.5 * u @ (g0 + o.b) - U) <= 1e-12 * abs(U)
+
+
+@pytest.mark.parametrize("flag_m", [1, 0])
+def test_laminate_with_isotropic_inclusion_layers(flag_m):
+    """Laminates that include the inclusion phase (isotropic, from E1 and nu1)
+    and, for flag_m = 0, the isotropic (Voigt-Reuss-Hill) matrix phases: the
+    closed form holds for any stiffness per layer, so these pin the phase
+    tables of both material modes."""
+    import analytic as AN
+
+    rng = np.random.default_rng(90 + flag_m)
+    shape, axis, ng = (5, 6, 14), 2, 3
+    layers = rng.integers(1, ng + 2, size=shape[axis])  # grains 1..ng and the inclusion ng+1
+    layers[:2] = [ng + 1, 1]
+    pix = AN.laminate_pix(shape, layers, axis)
+    rod = rng.normal(size=3 * ng)
+    s = np.array([4e-4, 1e-3, -2e-4, 1e-4, 3e-4, -2e-4])
+    p = O.Problem(*shape, ng + 1, flag_m=flag_m, c11=240e9, c12=150e9, c44=120e9, e1=380e9, nu1=0.27,
+                  exx=s[0], eyy=s[1], ezz=s[2], exz=s[3], eyz=s[4], exy=s[5], tol=1e-10, criterion=1)
+    r = O.run(p, pix, rod)
+    cm = O.Oracle(p, pix, rod).femat().cmod_array()
+    w, sig, _ = AN.laminate_exact(cm, layers, AN.engineering(s), axis)
+    assert r["exit_reason"] == 0
+    assert abs(r["utot"] - w * p.ns) <= 1e-12 * w * p.ns
+    assert _rel(r["strav"], sig) < 1e-12
