@@ -143,9 +143,11 @@ T* carve(char*& p, size_t count) {
 }
 
 // Fills the RVE's device tables: upload pix (to 0-based), phase materials,
-// phase kernel, block-Jacobi.  `base` must hold rve_bytes().
+// phase kernel, block-Jacobi.  `base` must hold rve_bytes().  checked: the phase
+// ids were range-checked already (at submission), so the map is copied as it is
+// and made 0-based on the device.
 int32_t setup_rve(RveDev& R, char* base, const e3d_rve_t& in, double e1, double nu1, cudaStream_t s,
-                  std::vector<int32_t>& scratch) {
+                  std::vector<int32_t>& scratch, bool checked = false) {
   R.nx = in.nx;
   R.ny = in.ny;
   R.nz = in.nz;
@@ -160,11 +162,13 @@ int32_t setup_rve(RveDev& R, char* base, const e3d_rve_t& in, double e1, double 
   R.dkd = carve<double>(p, 72 * (size_t)R.nphase);
   R.minv32 = carve<float>(p, 6 * R.ns);
   R.mats = carve<PhaseMat>(p, R.nphase);
-  scratch.resize((size_t)R.ns);
-  for (long long m = 0; m < R.ns; ++m) {
-    const int v = in.pix[m];
-    if (v < 1 || v > R.nphase) return E3D_ERR_INPUT;
-    scratch[(size_t)m] = v - 1;
+  if (!checked) {
+    scratch.resize((size_t)R.ns);
+    for (long long m = 0; m < R.ns; ++m) {
+      const int v = in.pix[m];
+      if (v < 1 || v > R.nphase) return E3D_ERR_INPUT;
+      scratch[(size_t)m] = v - 1;
+    }
   }
   std::vector<PhaseMat> mats((size_t)R.nphase);
   for (int g = 0; g < R.nphase; ++g) {
@@ -177,7 +181,12 @@ int32_t setup_rve(RveDev& R, char* base, const e3d_rve_t& in, double e1, double 
     M.G1 = e1 / 2.0 / (1.0 + nu1);
     for (int d = 0; d < 3; ++d) M.r[d] = M.pore ? 0.0 : in.rodrigues[3 * g + d];
   }
-  BCUDA(cudaMemcpyAsync(R.pix, scratch.data(), 4 * R.ns, cudaMemcpyHostToDevice, s));
+  if (checked) {
+    BCUDA(cudaMemcpyAsync(R.pix, in.pix, 4 * R.ns, cudaMemcpyHostToDevice, s));
+    pix_to_zero_based_kernel<<<(unsigned)((R.ns + 255) / 256), 256, 0, s>>>(R.ns, R.nphase, R.pix, nullptr);
+  } else {
+    BCUDA(cudaMemcpyAsync(R.pix, scratch.data(), 4 * R.ns, cudaMemcpyHostToDevice, s));
+  }
   BCUDA(cudaMemcpyAsync(R.mats, mats.data(), sizeof(PhaseMat) * mats.size(), cudaMemcpyHostToDevice, s));
   batch_phase_kernel<<<R.nphase, 32, 0, s>>>(R.mats, R.nphase, R.cmod, R.cs64, R.cs32, R.dk, R.dkd);
   GridDims G = job_dims(R.nx, R.ny, R.nz, 1);
@@ -762,13 +771,18 @@ int32_t e3d_serve_submit(e3d_server_t* s, const e3d_rve_t* rve, const double str
     return E3D_ERR_INPUT;
   const long long ns = (long long)rve->nx * rve->ny * rve->nz;
   // the phase-id range check of ppixel_hdf5 (src/elas3dxtal_pcg.f90:2986-2989),
-  // at submission so that a bad request is refused before it takes a slot
-  for (long long m = 0; m < ns; ++m)
-    if (rve->pix[m] < 1 || rve->pix[m] > rve->ngrains + 1) return E3D_ERR_INPUT;
+  // at submission so that a bad request is refused before it takes a slot; the
+  // server keeps its own copy of the map, checked as it is copied
   ServeJob* j = new ServeJob();
+  j->pix.assign(rve->pix, rve->pix + ns);
+  const int32_t hi = rve->ngrains + 1;
+  for (const int32_t v : j->pix)
+    if (v < 1 || v > hi) {
+      delete j;
+      return E3D_ERR_INPUT;
+    }
   j->id = s->next_id++;
   j->rve = *rve;
-  j->pix.assign(rve->pix, rve->pix + ns);
   j->rod.assign(rve->rodrigues, rve->rodrigues + 3 * (size_t)rve->ngrains);
   j->rve.pix = j->pix.data();
   j->rve.rodrigues = j->rod.data();
@@ -809,7 +823,7 @@ int32_t e3d_serve_step(e3d_server_t* s, int32_t* pending) {
     const long long ns = (long long)j->rve.nx * j->rve.ny * j->rve.nz;
     char* base = p;
     p += rve_bytes(ns, j->rve.ngrains + 1);
-    int32_t rc = setup_rve(j->R, base, j->rve, s->opts.e1, s->opts.nu1, s->stream, s->scratch);
+    int32_t rc = setup_rve(j->R, base, j->rve, s->opts.e1, s->opts.nu1, s->stream, s->scratch, true);
     if (rc) {
       j->done = true;
       j->result.status = E3D_EXIT_BREAKDOWN;

@@ -1156,12 +1156,13 @@ static __global__ void pix_from_device_kernel(long long ns, const int32_t* __res
 }
 
 // The same check and conversion in place: the 1-based ids were copied into
-// the phase map as they came from the host.
+// the phase map as they came from the host (err may be null when the host has
+// checked the ids already).
 static __global__ void pix_to_zero_based_kernel(long long ns, int nphase, int32_t* pix, int* err) {
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (long long)gridDim.x * blockDim.x) {
     const int32_t v = pix[m];
     if (v < 1 || v > nphase) {
-      atomicExch(err, DEV_BAD_INDEX);
+      if (err) atomicExch(err, DEV_BAD_INDEX);
       pix[m] = 0;
     } else {
       pix[m] = v - 1;
