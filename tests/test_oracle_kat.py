@@ -360,3 +360,29 @@ def test_laminate_with_isotropic_inclusion_layers(flag_m):
     assert r["exit_reason"] == 0
     assert abs(r["utot"] - w * p.ns) <= 1e-12 * w * p.ns
     assert _rel(r["strav"], sig) < 1e-12
+
+
+def test_laminate_effective_stiffness_matches_six_oracle_solves():
+    """tests/analytic.py's exact 6x6 laminate stiffness (used against the batch
+    engine on the GPU) equals the oracle's <sigma> over the six unit load cases
+    and is symmetric positive definite."""
+    import analytic as AN
+
+    rng = np.random.default_rng(140)
+    shape, axis, ng = (5, 13, 4), 1, 3
+    layers = rng.integers(1, ng + 1, size=shape[axis])
+    pix = AN.laminate_pix(shape, layers, axis)
+    rod = rng.normal(size=3 * ng)
+    cols = []
+    for lc in range(6):
+        s = np.zeros(6)
+        s[lc] = 1e-3 if lc < 3 else 0.5e-3
+        p = O.Problem(*shape, ng + 1, c11=240e9, c12=150e9, c44=100e9, exx=s[0], eyy=s[1], ezz=s[2], exz=s[3],
+                      eyz=s[4], exy=s[5], tol=1e-10, criterion=1)
+        cols.append(O.run(p, pix, rod)["strav"] / 1e-3)
+    ceff = np.stack(cols, axis=1)
+    cm = O.rotate_stiffness(rod, 240e9, 150e9, 100e9)
+    exact = AN.laminate_ceff(cm, layers, axis)
+    assert np.abs(ceff - exact).max() <= 1e-10 * np.abs(exact).max()
+    assert np.abs(exact - exact.T).max() <= 1e-12 * np.abs(exact).max()
+    assert np.linalg.eigvalsh(0.5 * (exact + exact.T)).min() > 0
